@@ -1,0 +1,307 @@
+"""Benchmark of the batched candidate-evaluation engine (one JSON line on stdout).
+
+Workload (default, "c1"): full 13-parameter identification of the Go2 model in FP32,
+4096 theta samples x 256 logged windows x horizon 20 control steps (4 physics
+substeps each) per CEM iteration; ground truth drawn from the parameter priors with a
+fixed seed and generated on the GPU (synthetic data: the reference's logged datasets
+are not available). One bench step is one CEM iteration: rollouts + windowed cost +
+elite refit + resampling, all on the device.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``--impl reference`` times the reference path's CPU restatement (the FP64 NumPy
+oracle; Isaac Gym cannot be installed) on the host cores on a bounded sample of the
+same workload. Under torchrun (N > 1) every rank runs an independent replica job
+(the path has no cross-job exchange); rank 0 prints.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT, ROOT / "spi-active_gb300"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+METRIC = "rollout-steps/s"
+C1 = dict(n_theta=4096, n_windows=256, horizon=20, n_params=13, iterations=30, elite_frac=0.1)
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# --------------------------------------------------------------------------------------
+# CPU baseline: the FP64 oracle on the host cores (spawned workers, no GPU in them)
+# --------------------------------------------------------------------------------------
+def _oracle_chunk(args):
+    seed, n_theta, n_windows, horizon = args
+    sys.path.insert(0, str(ROOT))
+    from oracle import dynamics as dyn
+    from oracle import go2_model as gm
+    from oracle import sysid as osy
+    rng = np.random.default_rng(seed)
+    th = gm.THETA_PRIOR_LO + (gm.THETA_PRIOR_HI - gm.THETA_PRIOR_LO) * rng.random((n_theta, 13))
+    x0 = np.tile(osy.standing_state(n_windows, z=0.30), (n_theta, 1))
+    acts = rng.normal(size=(n_windows, horizon, 12))
+    t0 = time.perf_counter()
+    dyn.rollout(x0, np.tile(acts, (n_theta, 1, 1)), np.repeat(th, n_windows, 0), gm.SimParams())
+    return n_theta * n_windows * horizon, time.perf_counter() - t0
+
+
+def cpu_baseline(seconds: float, horizon: int):
+    """Rollout-steps/s of the FP64 oracle over all host cores on a bounded C1 sample."""
+    import multiprocessing as mp
+    cores = os.cpu_count() or 1
+    per_task = (8, 32, horizon)          # 8 theta x 32 windows x H per task (256 rollouts)
+    ctx = mp.get_context("spawn")
+    done_steps, tasks = 0, 0
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        pool.map(_oracle_chunk, [(i, 1, 8, 2) for i in range(cores)])   # import warm-up
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < seconds:
+            res = pool.map(_oracle_chunk, [(1000 + tasks + i, *per_task) for i in range(cores)])
+            tasks += cores
+            done_steps += sum(r[0] for r in res)
+        wall = time.perf_counter() - t0
+    return {"value": done_steps / wall, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"{tasks} tasks x (8 theta x 32 windows x H={horizon}) of the c1 workload, "
+                      f"{done_steps} rollout-steps in {wall:.1f} s (FP64 NumPy oracle, spawn pool)"}
+
+
+# --------------------------------------------------------------------------------------
+# GPU clocks during the timed region
+# --------------------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------------------
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return None, 0, 1, 0
+    import torch
+    import torch.distributed as dist
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return dist, dist.get_rank(), ws, local
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    base = cpu_baseline(args.cpu_seconds, C1["horizon"])
+    line = {"metric": METRIC, "value": base["value"], "unit": METRIC, "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": C1["n_theta"] * C1["n_windows"] * C1["horizon"] / base["value"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": "c1: 4096 theta x 256 windows x H=20, 13 params, "
+                                                        "Go2 FP64 NumPy oracle on host cores"},
+            "cpu_baseline": base,
+            "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    dist, rank, ws, local = _dist()
+    import __graft_entry__
+    if rank == 0:
+        __graft_entry__.build()
+    if dist:
+        dist.barrier()
+    from spi_gb300 import robot
+    from spi_gb300.cem import CEM
+    from spi_gb300.data import synthetic_windows
+    from spi_gb300.engine import Engine, probe_fp32_peak
+    from spi_gb300.flops import flops_per_rollout_step
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    cfg = robot.SimConfig()
+    N, W, H = C1["n_theta"], C1["n_windows"], C1["horizon"]
+    rng = np.random.default_rng(1234 + rank)
+    lo, hi = robot.THETA_PRIOR_LO, robot.THETA_PRIOR_HI
+    theta_true = lo + (hi - lo) * rng.random(13)
+    eng = Engine(cfg, device=dev)
+    init, actions, target = synthetic_windows(eng, theta_true, W, H, seed=77 + rank)
+    eng.load_windows(torch.from_numpy(init), torch.from_numpy(actions), torch.from_numpy(target))
+    cem = CEM(eng, n_samples=N, param_ids=list(range(13)), lo=lo, hi=hi, nominal=robot.THETA_NOMINAL,
+              elite_frac=C1["elite_frac"], seed=4321 + rank)
+    flush = torch.empty(256 * 1024 * 1024 // 4, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    for _ in range(args.warmup):
+        cem.step()
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    run_s = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    run_e = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.zero_()                                  # L2 flush between timed steps
+            starts[k].record(stream)
+            cem.step(rollout_events=(run_s[k], run_e[k]))
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    kern_ms = [s.elapsed_time(e) for s, e in zip(run_s, run_e)]
+    total_ms = float(np.sum(step_ms))
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    n_bad = eng.sync()
+    steps_per_iter = N * W * H
+    value = ws * steps_per_iter * args.steps / (total_ms * 1e-3)
+
+    # end to end: host buffers through the public API, copies inside the timed region
+    e2e = None
+    if not args.no_e2e:
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()   # noqa: E731
+        h_init, h_act, h_tgt = pin(init), pin(actions), pin(target)
+        h_theta = pin(cem.sample_host(args.steps))
+        h_cost = torch.empty((N,), dtype=torch.float32).pin_memory()
+        d_init = torch.empty_like(h_init, device=dev)
+        d_act = torch.empty_like(h_act, device=dev)
+        d_tgt = torch.empty_like(h_tgt, device=dev)
+        d_theta = torch.empty((N, 13), device=dev)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for k in range(args.steps):
+            d_init.copy_(h_init, non_blocking=True)
+            d_act.copy_(h_act, non_blocking=True)
+            d_tgt.copy_(h_tgt, non_blocking=True)
+            d_theta.copy_(h_theta[k], non_blocking=True)
+            eng.load_windows(d_init, d_act, d_tgt)
+            eng.set_theta(d_theta)
+            eng.run()
+            _, cost = eng.read()
+            h_cost.copy_(cost, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = e0.elapsed_time(e1)
+        h2d = (init.nbytes + actions.nbytes + target.nbytes + N * 13 * 4)
+        e2e = {"value": ws * steps_per_iter * args.steps / (e2e_ms * 1e-3), "unit": METRIC,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(N * 4),
+               "note": "per step: windows + theta H2D from pinned memory, spi_load_windows, "
+                       "spi_set_theta, spi_run, spi_read_costs, cost D2H (evaluation only)"}
+
+    fl = flops_per_rollout_step(cfg)
+    kmean = float(np.mean(kern_ms))
+    peak = probe_fp32_peak()
+    achieved = steps_per_iter * fl / (kmean * 1e-3)
+    roof = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+            "frac": achieved / peak, "traffic": None,
+            "kernel": "rollout_kernel (+finalize_costs)", "kernel_ms": kmean,
+            "flops_per_rollout_step": fl,
+            "peak_source": "measured FP32 FMA-loop probe on this GPU (no FP32 entry in MEASURED_PEAKS.json)"}
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "c1", "n_theta": N, "n_windows": W, "horizon": H, "substeps": cfg.decimation,
+                       "n_params": 13, "elite_frac": C1["elite_frac"],
+                       "step": "one CEM iteration (rollouts + cost + refit + resample)",
+                       "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{ws}"},
+            "roofline": roof, "e2e": e2e, "gpu_launches": cem.launches_per_step * args.steps,
+            "wall_s": wall, "nonfinite_rollouts": n_bad, "clocks": clocks.summary(),
+            "cem": {"best_cost": cem.best_cost(), "theta_err": cem.theta_error(theta_true)}}
+    if ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds, H)
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,169 @@
+/*
+ * spi_engine.h -- C ABI of the GB300 batched candidate-evaluation engine.
+ *
+ * Drop-in for the replay-evaluation path of SPI-Active. The reference
+ * evaluates one parameter vector theta at a time across Isaac Gym envs; this
+ * engine evaluates a batch of theta samples against a batch of logged windows
+ * in one launch. Every call returns an int status (SPI_OK or a negative
+ * SPI_E* code; spi_last_error() gives the message). Pointers documented as
+ * "device" are CUDA device pointers owned by the caller (e.g. torch
+ * data_ptr()); the engine never frees caller memory. An engine is bound to
+ * one CUDA stream; calls are thread-compatible, not thread-safe.
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   spi_create        <- scripts/eval.py:313-321 instantiate_env (env + sim creation)
+ *   spi_load_windows  <- scripts/eval.py:174-182 to_device, plus the per-chunk reset of
+ *                        evaluate_batch :243-277 (root state / dof state written from the window)
+ *   spi_set_theta     <- scripts/eval.py:204-214 apply_base_mass and
+ *                        spigym/simulator/isaacgym/isaacgym_active_sysid.py:39-95 set_<param>
+ *   spi_run           <- scripts/eval.py:217-310 evaluate_batch (H x env.step, final-step
+ *                        errors, masked sums, normaliser)
+ *   spi_read_costs    <- the MassEvalResult of scripts/eval.py:38-42 / :306-310 and
+ *                        scripts/mass_opt.py:62-76 compute_cost
+ *   spi_run_trace     <- reading simulator.robot_root_states / dof_state after every
+ *                        env.step (spigym/simulator/isaacgym/isaacgym.py:567-577)
+ *   spi_cem_*         <- the Optuna ask/tell loop of scripts/mass_opt.py:203-219
+ *                        (TPE there; CEM here, on the device)
+ */
+#ifndef SPI_ENGINE_H
+#define SPI_ENGINE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPI_ABI_VERSION 1
+
+#define SPI_OK 0
+#define SPI_EINVAL (-1)      /* bad argument or size */
+#define SPI_ENOMEM (-2)      /* device allocation failed */
+#define SPI_ECUDA (-3)       /* CUDA runtime error */
+#define SPI_ESTATE (-4)      /* call out of order (e.g. run before load) */
+#define SPI_ETIMEOUT (-5)    /* a bounded device wait ran out */
+#define SPI_EBUDGET (-6)     /* request exceeds the admission budget */
+
+#define SPI_STATE_DIM 37     /* pos3 quat4(xyzw) linvel3 angvel3 (world) q12 qd12 */
+#define SPI_THETA_DIM 13
+#define SPI_N_JOINTS 12
+#define SPI_N_LEG_BODIES 12
+#define SPI_N_COMP 9         /* |dp| |dquat| |dq| |dp|^2 |dquat|^2 |dv|^2 |dw|^2 |dq|^2 |dqd|^2 */
+
+/* theta slots: 0 base mass [kg]; 1-3 base CoM offset [m]; 4 base inertia-diagonal scale;
+ * 5-8 front legs (FL, FR): Kp scale, Coulomb friction [N m], armature [kg m^2], torque-limit
+ * scale; 9-12 rear legs (RL, RR): the same four. */
+
+/* Robot model and simulation settings. Leg bodies are ordered FL, FR, RL, RR x hip, thigh,
+ * calf (the Isaac Gym DFS order of spigym/config/robot/go2/go2.yaml:29); hip joints rotate
+ * about x, thigh and calf joints about y. Inertias are 6 floats xx yy zz xy xz yz. */
+typedef struct spi_robot {
+    float body_origin[SPI_N_LEG_BODIES][3]; /* joint origin in the parent frame */
+    float body_mass[SPI_N_LEG_BODIES];
+    float body_h[SPI_N_LEG_BODIES][3];      /* mass * CoM (body frame) */
+    float body_I[SPI_N_LEG_BODIES][6];      /* rotational inertia about the body origin */
+    float base_mass_nominal;
+    float base_com[3];                      /* nominal base CoM; theta[1:4] offsets it */
+    float base_Ic[6];                       /* nominal base inertia about its CoM */
+    float fixed_mass;                       /* collapsed fixed links on the base (heads) */
+    float fixed_h[3];
+    float fixed_I[6];                       /* about the base origin */
+    float foot[3];                          /* foot contact point in the calf frame */
+    float foot_radius;
+    float corners[8][3];                    /* base collision-box corners (base frame) */
+    float contact_k, contact_c, contact_ct, contact_mu;
+    float contact_ramp;                     /* penetration over which the normal damping fades in [m] */
+    float kp[SPI_N_JOINTS], kd[SPI_N_JOINTS];
+    float kd_scale, action_scale, action_clip, hip_action_scale;
+    float default_q[SPI_N_JOINTS], torque_limit[SPI_N_JOINTS], velocity_limit[SPI_N_JOINTS];
+    float motor_gain[3];                    /* per joint type hip/thigh/calf, after the clip */
+    float tanh_a[3];                        /* a*tanh(tau/a) per joint type; 0 disables */
+    float friction_vel;                     /* Coulomb friction tanh width [rad/s] */
+    float sim_dt;                           /* physics substep [s] */
+    float gravity;
+    int32_t decimation;                     /* substeps per control step */
+    int32_t torque_speed;                   /* torque limit falls linearly to 0 at velocity_limit */
+    int32_t base_contact;                   /* base box corners collide */
+    int32_t inertia_follows_mass;           /* base inertia scales with mass/nominal */
+} spi_robot;
+
+typedef struct spi_engine spi_engine;
+
+int spi_abi_version(void);
+/* Message of the last failing call on this thread ("" if none). */
+const char* spi_last_error(void);
+
+int spi_create(const spi_robot* robot, spi_engine** out);
+int spi_destroy(spi_engine* e);
+/* Bind the engine to a cudaStream_t (NULL = legacy default stream). */
+int spi_set_stream(spi_engine* e, void* stream);
+
+/* Windows, device pointers in the reference's row layout: init and target [W][37] states,
+ * actions [W][H][12] (raw policy actions, clipped and scaled inside), weight [W] per-window
+ * weight (NULL = all 1), norm = divisor of the weighted sums (the reference's count of
+ * non-end windows; <= 0 means W). Copied into engine-owned structure-of-arrays storage. */
+int spi_load_windows(spi_engine* e, const float* init, const float* actions,
+                     const float* target, const float* weight, int W, int H, float norm);
+
+/* Theta batch, device [N][13]. Copied into engine storage. */
+int spi_set_theta(spi_engine* e, const float* theta, int N);
+
+/* Cost weights: mode 0 = reference L2 (10/5/1 on |dp|, |dquat|, |dq|; scripts/mass_opt.py:28-32),
+ * mode 1 = weighted squared error with sq_weights[6] (pos, quat, linvel, angvel, q, qd). */
+int spi_set_cost(spi_engine* e, int mode, const float* sq_weights);
+
+/* Roll every (theta, window) pair H control steps and reduce the windowed cost. Async. */
+int spi_run(spi_engine* e);
+/* Same, also writing every control step's state to trace, device [N][W][H][37]. */
+int spi_run_trace(spi_engine* e, float* trace);
+
+/* Copy results of the last run (async on the engine stream): comp device [N][9] mean
+ * components (may be NULL), cost device [N] scalar cost (may be NULL). */
+int spi_read_costs(spi_engine* e, float* comp, float* cost);
+
+/* Copy the current theta batch [N][13] to theta (device or pinned host), async. */
+int spi_read_theta(spi_engine* e, float* theta);
+
+/* Wait for the engine stream; report rollouts whose final state was not finite. */
+int spi_sync(spi_engine* e, int64_t* n_nonfinite);
+
+/* ---- cross-entropy-method identification on the device -------------------------------
+ * Replaces the host-side Optuna ask/tell loop of scripts/mass_opt.py:203-219 (TPE) and the
+ * grid of scripts/mass_landscape.py:153 with a CEM whose sampling, elite selection, mean /
+ * covariance refit and FP64 Cholesky run on the GPU. The engine's theta batch becomes the
+ * CEM population; slots not identified keep their nominal value. */
+typedef struct spi_cem_config {
+    int32_t n_samples;                       /* population N (2 .. 16384) */
+    int32_t dim;                             /* identified parameters P (1 .. 13) */
+    int32_t param_ids[SPI_THETA_DIM];        /* theta slot of each identified parameter */
+    float nominal[SPI_THETA_DIM];            /* values of the other slots */
+    double lo[SPI_THETA_DIM], hi[SPI_THETA_DIM];  /* prior box per identified parameter */
+    double elite_frac;                       /* elites = max(2, floor(elite_frac * N + 0.5)) */
+    double alpha;                            /* smoothing of mean and covariance (1 = none) */
+    double min_std_frac;                     /* per-dimension std floor, fraction of hi - lo */
+    uint64_t seed;                           /* Philox4x32-10 key */
+    int32_t job_id;                          /* Philox counter word 3 */
+} spi_cem_config;
+
+int spi_cem_init(spi_engine* e, const spi_cem_config* cfg);
+/* Draw this iteration's population into the theta batch (iteration 0: uniform prior box). */
+int spi_cem_sample(spi_engine* e);
+/* Refit from the last run's costs; iteration += 1. */
+int spi_cem_refit(spi_engine* e);
+/* sample + run + refit, all asynchronous on the engine stream. */
+int spi_cem_step(spi_engine* e);
+/* `iterations` steps; with use_graph one step is captured once as a CUDA graph and replayed. */
+int spi_cem_run(spi_engine* e, int iterations, int use_graph);
+/* Synchronous read of the distribution (host pointers, any may be NULL): mu [P],
+ * cov [P][P], best theta [13] and cost over all iterations, iterations done. */
+int spi_cem_read(spi_engine* e, double* mu, double* cov, float* best_theta, float* best_cost,
+                 int32_t* iteration);
+
+/* Upper bound of the FP32 throughput of this GPU, measured by an FMA loop [FLOP/s]. */
+int spi_probe_fp32_peak(double* flops_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPI_ENGINE_H */

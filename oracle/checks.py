@@ -12,11 +12,13 @@ from .dynamics import _I_RIGID, _ORIGIN, _unit, base_inertia, quat_to_R
 from .spatial import crf, crm, mv, plucker, rot_axis
 
 
-def rnea(x, a0_true, qdd, theta, sim, fext=None, gravity=True):
+def rnea(x, a0_true, qdd, theta, sim, fext=None, gravity=True, I_extra=None):
     """Floating-base RNEA. Returns (base wrench [B,6], joint torques [B,12]).
 
     a0_true is the base spatial acceleration in base coordinates (Featherstone
-    convention, gravity not removed); fext is a list of 13 [B,6] body-frame forces.
+    convention, gravity not removed); fext is a list of 13 [B,6] body-frame forces;
+    I_extra an optional list of 13 [B,6,6] inertias acting on the true accelerations
+    (the implicit contact-damping terms).
     """
     B = x.shape[0]
     quat, vw, ww = x[:, 3:7], x[:, 7:10], x[:, 10:13]
@@ -39,10 +41,19 @@ def rnea(x, a0_true, qdd, theta, sim, fext=None, gravity=True):
         v[i] = mv(X[i], v[lam]) + S * qd[:, j:j + 1]
         a[i] = mv(X[i], a[lam]) + S * qdd[:, j:j + 1] + mv(crm(v[i]), S * qd[:, j:j + 1])
         I[i] = np.broadcast_to(_I_RIGID[i], (B, 6, 6))
+    # true (unshifted) body accelerations for the implicit-damping terms
+    at = [None] * nb
+    at[0] = a0_true
+    for i in range(1, nb):
+        lam, ax, j = gm.PARENT[i], gm.AXIS[i], i - 1
+        S = _unit(ax)[None, :]
+        at[i] = mv(X[i], at[lam]) + S * qdd[:, j:j + 1] + mv(crm(v[i]), S * qd[:, j:j + 1])
     for i in range(nb):
         f[i] = mv(I[i], a[i]) + mv(crf(v[i]), mv(I[i], v[i]))
         if fext is not None:
             f[i] = f[i] - fext[i]
+        if I_extra is not None:
+            f[i] = f[i] + mv(I_extra[i], at[i])
     tau = np.zeros((B, gm.N_JOINTS))
     for i in range(nb - 1, 0, -1):
         lam, ax, j = gm.PARENT[i], gm.AXIS[i], i - 1

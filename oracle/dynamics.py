@@ -18,8 +18,11 @@ Test infrastructure (the checker of the CUDA rollout kernel). Equations:
   in legged_robot_base.py:201-209.
 * Dynamics: floating-base articulated-body algorithm (Featherstone), penalty
   contact at the four foot spheres (r = 0.022 m) and the eight corners of the
-  base collision box: fn = max(0, k*pen - c*vz) for pen > 0, tangential force
-  -min(ct*|vt|, mu*fn) * vt/|vt|. Semi-implicit Euler on the base's
+  base collision box: fn = max(0, k*pen - c*s(pen)*vz) for pen > 0 with the
+  damping ramp s = min(1, pen/ramp), tangential force -min(ct*|vt|, mu*fn) *
+  vt/|vt|. Contact damping is linearly implicit: an active contact point adds a
+  point mass dt*max(c, ct)*s(pen) at the contact to its body's inertia in the
+  ABA (exact for linear damping; keeps the stiff contact mode stable). Semi-implicit Euler on the base's
   body-coordinate spatial velocity and the joint velocities; the orientation is
   advanced with the new body angular velocity (q <- normalise(q + dt/2 q (x) w_b))
   and the new body velocity is mapped to world coordinates with the new pose. Root state layout follows the reference's root-state rows
@@ -94,10 +97,21 @@ def motor_torques(q, qd, action, theta, sim: gm.SimParams):
     return tau, arm
 
 
+def damping_ramp(pen, sim: gm.SimParams):
+    """Fraction of the contact damping active at penetration pen (0 at touchdown, 1 past the ramp)."""
+    return np.clip(pen / sim.contact_ramp, 0.0, 1.0)
+
+
+def implicit_mass(pen, sim: gm.SimParams):
+    """Point mass dt*c_imp*ramp added at a contact point: linearly implicit contact damping."""
+    return sim.sim_dt * max(sim.contact_c, sim.contact_ct) * damping_ramp(pen, sim)
+
+
 def foot_force(p_foot, v_foot, sim: gm.SimParams, radius=None):
     """Penalty contact force (world frame) on a contact point (foot sphere or box corner)."""
     pen = (sim.foot_radius if radius is None else radius) - p_foot[..., 2]
-    fn = np.where(pen > 0, np.maximum(0.0, sim.contact_k * pen - sim.contact_c * v_foot[..., 2]), 0.0)
+    fn = np.where(pen > 0, np.maximum(0.0, sim.contact_k * pen
+                                      - sim.contact_c * damping_ramp(pen, sim) * v_foot[..., 2]), 0.0)
     vt = v_foot[..., :2]
     vtn = np.sqrt(np.sum(vt * vt, -1))
     lim = sim.contact_mu * fn
@@ -150,6 +164,7 @@ def substep(x, action, theta, sim: gm.SimParams, return_aux=False, tau_override=
         pw[i] = pw[lam] + mv(Rw[lam], np.broadcast_to(_ORIGIN[i], (B, 3)))
 
     fext = [np.zeros((B, 6)) for _ in range(nb)]
+    I_imp = [np.zeros((B, 6, 6)) for _ in range(nb)]   # implicit contact damping
     foot_F = np.zeros((B, 4, 3))
     for l, i in enumerate(CALVES):
         r = np.broadcast_to(gm.FOOT_IN_CALF, (B, 3))
@@ -160,6 +175,7 @@ def substep(x, action, theta, sim: gm.SimParams, return_aux=False, tau_override=
         foot_F[:, l] = F
         fl = mv(np.swapaxes(Rw[i], -1, -2), F)
         fext[i] = np.concatenate([np.cross(r, fl), fl], -1)
+        I_imp[i] = rigid_inertia(implicit_mass(sim.foot_radius - pf[:, 2], sim), r, np.zeros((B, 3, 3)))
 
     if sim.base_contact:
         for corner in gm.BASE_CORNERS:
@@ -169,6 +185,7 @@ def substep(x, action, theta, sim: gm.SimParams, return_aux=False, tau_override=
             F = foot_force(pc, mv(R, vcb), sim, radius=0.0)
             fl = mv(Rt, F)
             fext[0] = fext[0] + np.concatenate([np.cross(r, fl), fl], -1)
+            I_imp[0] = I_imp[0] + rigid_inertia(implicit_mass(-pc[:, 2], sim), r, np.zeros((B, 3, 3)))
 
     IA = [None] * nb
     pA = [None] * nb
@@ -180,6 +197,11 @@ def substep(x, action, theta, sim: gm.SimParams, return_aux=False, tau_override=
         if i > 0:
             IA[i] = np.broadcast_to(_I_RIGID[i], (B, 6, 6)).copy()
         pA[i] = mv(crf(v[i]), mv(IA[i], v[i])) - fext[i]
+        # the implicit term acts on the true acceleration; the ABA runs in the gravity-shifted
+        # frame (a' = a - (0, g)), so the shift's share I_imp (0, g_i) joins the bias
+        g_i = mv(np.swapaxes(Rw[i], -1, -2), np.broadcast_to(np.array([0.0, 0.0, -sim.gravity]), (B, 3)))
+        pA[i] = pA[i] + mv(I_imp[i], np.concatenate([np.zeros((B, 3)), g_i], -1))
+        IA[i] = IA[i] + I_imp[i]
 
     U = [None] * nb
     D = [None] * nb
@@ -222,7 +244,8 @@ def substep(x, action, theta, sim: gm.SimParams, return_aux=False, tau_override=
     q_n = q + dt * qd_n
     xn = np.concatenate([p_n, quat_n, vw_n, ww_n, q_n, qd_n], -1)
     if return_aux:
-        return xn, dict(a0=a0, qdd=qdd, tau=tau, foot_force=foot_F, v=v, Rw=Rw, pw=pw)
+        return xn, dict(a0=a0, qdd=qdd, tau=tau, foot_force=foot_F, v=v, Rw=Rw, pw=pw, I_imp=I_imp,
+                        fext=fext)
     return xn
 
 

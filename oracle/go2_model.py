@@ -144,6 +144,7 @@ class SimParams:
     contact_c: float = 200.0          # N s/m (normal damping)
     contact_ct: float = 200.0         # N s/m (tangential viscous slope, capped at mu*fn)
     contact_mu: float = 0.8
+    contact_ramp: float = 1e-3        # m: normal damping fades in over the first mm of penetration
     foot_radius: float = FOOT_RADIUS
     base_contact: bool = True          # base box corners collide with the ground
     kp: np.ndarray = field(default_factory=lambda: np.full(12, 20.0))

@@ -1,0 +1,192 @@
+// cem.cuh -- cross-entropy-method refit and sampling on the device.
+//
+// Per job: the population theta [N][13] (float), its costs [N]; the distribution
+// (mean, covariance, Cholesky factor) in FP64. One refit = sort (cost, index) keys
+// (NaN last; ties by index), mean and covariance of the n_elite best, smoothing
+// alpha, per-dimension std floor, FP64 Cholesky. Sampling: Philox4x32-10 words
+// (counter = sample, iteration, block, job; key = seed) -> Box-Muller normals ->
+// theta = clip(mu + L z, lo, hi); iteration 0 samples the prior box uniformly.
+// All iteration state lives on the device, so an iteration can be graph-captured.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cem_state.h"
+#include "spi_engine.h"
+
+namespace spi {
+
+__device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+    const uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+    c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+  }
+}
+
+__device__ __forceinline__ double u01(uint32_t w) { return ((double)w + 0.5) * 2.3283064365386963e-10; }
+
+// Orderable key: cost ascending (NaN last), then index ascending.
+__device__ __forceinline__ unsigned long long cost_key(float c, unsigned idx) {
+  uint32_t b = __float_as_uint(c);
+  uint32_t o;
+  if (isnan(c)) o = 0xFFFFFFFFu;
+  else o = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+  return ((unsigned long long)o << 32) | idx;
+}
+
+// Draw the population of the current iteration into theta [N][13].
+__global__ void cem_sample_kernel(CemState* __restrict__ st_all, int job_offset, float* __restrict__ theta_base,
+                                  const long long* __restrict__ theta_offsets) {
+  CemState* st = st_all + blockIdx.y;
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= st->n_samples) return;
+  float* theta = theta_base + (theta_offsets ? theta_offsets[blockIdx.y] : 0) + (size_t)n * SPI_THETA_DIM;
+  const int P = st->dim, it = st->iter;
+  const uint32_t k0 = (uint32_t)(st->seed & 0xFFFFFFFFull), k1 = (uint32_t)(st->seed >> 32);
+  double z[CEM_MAX_DIM + 3];
+#pragma unroll
+  for (int b = 0; b < (CEM_MAX_DIM + 3) / 4; ++b) {
+    if (4 * b >= P) break;
+    uint32_t c[4] = {(uint32_t)n, (uint32_t)it, (uint32_t)b, (uint32_t)(st->job + job_offset)};
+    philox4x32_10(c, k0, k1);
+    if (it == 0) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) z[4 * b + q] = u01(c[q]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const double u1 = u01(c[2 * q]), u2 = u01(c[2 * q + 1]);
+        const double r = sqrt(-2.0 * log(u1));
+        double s, co;
+        sincospi(2.0 * u2, &s, &co);
+        z[4 * b + 2 * q] = r * co;
+        z[4 * b + 2 * q + 1] = r * s;
+      }
+    }
+  }
+  float out[SPI_THETA_DIM];
+#pragma unroll
+  for (int i = 0; i < SPI_THETA_DIM; ++i) out[i] = st->nominal[i];
+  for (int d = 0; d < P; ++d) {
+    double v;
+    if (it == 0) {
+      v = st->lo[d] + (st->hi[d] - st->lo[d]) * z[d];
+    } else {
+      v = st->mu[d];
+      for (int e = 0; e <= d; ++e) v += st->L[d * CEM_MAX_DIM + e] * z[e];
+      v = fmin(fmax(v, st->lo[d]), st->hi[d]);
+    }
+    const int slot = st->param_ids[d];
+#pragma unroll
+    for (int i = 0; i < SPI_THETA_DIM; ++i)
+      if (i == slot) out[i] = (float)v;
+  }
+#pragma unroll
+  for (int i = 0; i < SPI_THETA_DIM; ++i) theta[i] = out[i];
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// One CTA (1024 threads) per job: elite select + mean / covariance + Cholesky.
+__global__ void __launch_bounds__(1024) cem_refit_kernel(CemState* __restrict__ st_all,
+                                                         const float* __restrict__ theta_base,
+                                                         const long long* __restrict__ theta_offsets,
+                                                         const float* __restrict__ cost_base,
+                                                         const long long* __restrict__ cost_offsets) {
+  extern __shared__ unsigned long long keys[];
+  __shared__ double s_mu[CEM_MAX_DIM];
+  __shared__ double s_cov[CEM_MAX_DIM * CEM_MAX_DIM];
+  CemState* st = st_all + blockIdx.x;
+  const float* theta = theta_base + (theta_offsets ? theta_offsets[blockIdx.x] : 0);
+  const float* cost = cost_base + (cost_offsets ? cost_offsets[blockIdx.x] : 0);
+  const int N = st->n_samples, P = st->dim, ne = st->n_elite;
+  int npad = 1;
+  while (npad < N) npad <<= 1;
+  for (int i = threadIdx.x; i < npad; i += blockDim.x)
+    keys[i] = i < N ? cost_key(cost[i], (unsigned)i) : ~0ull;
+  __syncthreads();
+  // bitonic sort, ascending
+  for (int k = 2; k <= npad; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < npad; i += blockDim.x) {
+        const int l = i ^ j;
+        if (l > i) {
+          const unsigned long long a = keys[i], b = keys[l];
+          const bool up = (i & k) == 0;
+          if ((a > b) == up) { keys[i] = b; keys[l] = a; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  // elite mean, one warp per dimension
+  for (int d = warp; d < P; d += nwarps) {
+    const int slot = st->param_ids[d];
+    double s = 0.0;
+    for (int e = lane; e < ne; e += 32) s += (double)theta[(size_t)(keys[e] & 0xFFFFFFFFull) * SPI_THETA_DIM + slot];
+    s = warp_sum_d(s);
+    if (lane == 0) s_mu[d] = s / ne;
+  }
+  __syncthreads();
+  // elite covariance, one warp per upper-triangle entry
+  const int nent = P * (P + 1) / 2;
+  for (int q = warp; q < nent; q += nwarps) {
+    int i = 0, r = q;
+    while (r >= P - i) { r -= P - i; ++i; }
+    const int j = i + r;
+    const int si = st->param_ids[i], sj = st->param_ids[j];
+    double s = 0.0;
+    for (int e = lane; e < ne; e += 32) {
+      const float* t = theta + (size_t)(keys[e] & 0xFFFFFFFFull) * SPI_THETA_DIM;
+      s += ((double)t[si] - s_mu[i]) * ((double)t[sj] - s_mu[j]);
+    }
+    s = warp_sum_d(s);
+    if (lane == 0) { s_cov[i * CEM_MAX_DIM + j] = s / ne; s_cov[j * CEM_MAX_DIM + i] = s / ne; }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double a = st->alpha;
+    for (int i = 0; i < P; ++i) st->mu[i] = a * s_mu[i] + (1.0 - a) * st->mu[i];
+    for (int i = 0; i < P; ++i)
+      for (int j = 0; j < P; ++j) {
+        double v = a * s_cov[i * CEM_MAX_DIM + j] + (1.0 - a) * st->cov[i * CEM_MAX_DIM + j];
+        if (i == j) v += st->min_std[i] * st->min_std[i];
+        st->cov[i * CEM_MAX_DIM + j] = v;
+      }
+    // Cholesky, lower
+    int ok = 1;
+    for (int j = 0; j < P; ++j) {
+      double d = st->cov[j * CEM_MAX_DIM + j];
+      for (int k = 0; k < j; ++k) d -= st->L[j * CEM_MAX_DIM + k] * st->L[j * CEM_MAX_DIM + k];
+      if (!(d > 0.0)) { ok = 0; d = st->min_std[j] * st->min_std[j]; }
+      const double ljj = sqrt(d);
+      st->L[j * CEM_MAX_DIM + j] = ljj;
+      for (int i = j + 1; i < P; ++i) {
+        double s = st->cov[i * CEM_MAX_DIM + j];
+        for (int k = 0; k < j; ++k) s -= st->L[i * CEM_MAX_DIM + k] * st->L[j * CEM_MAX_DIM + k];
+        st->L[i * CEM_MAX_DIM + j] = s / ljj;
+      }
+      for (int i = 0; i < j; ++i) st->L[i * CEM_MAX_DIM + j] = 0.0;
+    }
+    if (!ok) st->status = 1;
+    const unsigned b = (unsigned)(keys[0] & 0xFFFFFFFFull);
+    const float bc = cost[b];
+    if (bc < st->best_cost || (isnan(st->best_cost) && !isnan(bc))) {
+      st->best_cost = bc;
+      for (int i = 0; i < SPI_THETA_DIM; ++i) st->best_theta[i] = theta[(size_t)b * SPI_THETA_DIM + i];
+    }
+    st->iter += 1;
+  }
+}
+
+}  // namespace spi

@@ -1,0 +1,583 @@
+// dynamics.cuh -- one physics substep of the Go2 floating-base model, split per leg.
+//
+// Templated on the scalar type T so the same source builds (a) the sm_103a rollout
+// kernel (T = float, one lane per leg, four lanes per rollout) and (b) a host
+// emulation (T = double, or a flop-counting scalar) that runs the phases in sequence.
+//
+// Phases of a substep (leg l = 0..3, FL FR RL RR):
+//   A  per leg : motor torques, leg kinematics, foot + 2 base-corner contacts, ABA
+//               backward pass of the 3-body chain -> the leg's articulated inertia and
+//               bias force expressed at the base (LegOut, 27 values)
+//   (sum of the four LegOut: warp shuffles on the device, a loop on the host)
+//   B  base    : base articulated inertia + bias, 6x6 Cholesky solve for the base
+//               acceleration, semi-implicit Euler step of the floating base
+//   C  per leg : ABA forward pass (joint accelerations) and joint integration
+//
+// Equations (Featherstone spatial algebra, motion = (w; v), force = (n; f)):
+//   PD law  tau = kp_s*Kp*(action_scale*clip(a) + q0 - q) - kd_s*Kd*qd, clipped to
+//           +-ts*tau_lim*(1 - |qd|/qd_max)+ -- spigym/envs/legged_base_task/
+//           legged_robot_base.py:185-187, 542-560 (hip action x hip_scale: go2_omni.py:437)
+//   motor   per-type gain and a*tanh(tau/a) -- spigym/envs/sysid/active_sysid_openloop.py:365-400
+//   joint   friction -Fc*tanh(qd/w_f); armature added to the ABA joint inertia D
+//   contact fn = max(0, k*pen - c*s*vz) if pen > 0, s = min(1, pen/ramp) (damping fades in over
+//           the first `ramp` of penetration, so the force is continuous at touchdown);
+//           ft = -min(ct, mu*fn/|vt|)*vt. Contact damping is linearly implicit: an active
+//           contact adds a point mass dt*max(c, ct)*s at the contact point to its body's
+//           articulated inertia (exact for linear damping, stable at any dt)
+//   base    nu += dt*a;  q <- normalise(q + dt/2 q(x)w_b);  p += dt*R(q)*v_b
+#pragma once
+
+#include "spi_engine.h"
+
+#if defined(__CUDACC__)
+#define SPI_HD __host__ __device__
+#define SPI_INL __host__ __device__ __forceinline__
+#else
+#define SPI_HD
+#define SPI_INL inline
+#include <cmath>
+#endif
+
+namespace spi {
+
+// ---------------------------------------------------------------------------
+// scalar helpers (overloaded for float / double; the flop counter adds its own)
+// ---------------------------------------------------------------------------
+SPI_INL float m_sqrt(float x) { return sqrtf(x); }
+SPI_INL double m_sqrt(double x) { return sqrt(x); }
+SPI_INL float m_tanh(float x) { return tanhf(x); }
+SPI_INL double m_tanh(double x) { return tanh(x); }
+SPI_INL void m_sincos(float x, float* s, float* c) {
+#if defined(__CUDA_ARCH__)
+  sincosf(x, s, c);
+#else
+  *s = sinf(x); *c = cosf(x);
+#endif
+}
+SPI_INL void m_sincos(double x, double* s, double* c) { *s = sin(x); *c = cos(x); }
+SPI_INL float m_fabs(float x) { return fabsf(x); }
+SPI_INL double m_fabs(double x) { return fabs(x); }
+SPI_INL float m_fmax(float a, float b) { return fmaxf(a, b); }
+SPI_INL double m_fmax(double a, double b) { return fmax(a, b); }
+SPI_INL float m_fmin(float a, float b) { return fminf(a, b); }
+SPI_INL double m_fmin(double a, double b) { return fmin(a, b); }
+template <class T> SPI_INL T m_sel(bool c, T a, T b) { return c ? a : b; }
+template <class T> SPI_INL T m_clamp(T x, T lo, T hi) { return m_fmin(m_fmax(x, lo), hi); }
+
+// ---------------------------------------------------------------------------
+// small vector / matrix types
+// ---------------------------------------------------------------------------
+template <class T> struct V3 { T x, y, z; };
+template <class T> struct S3 { T xx, yy, zz, xy, xz, yz; };   // symmetric 3x3
+template <class T> struct M3 { T m[3][3]; };                  // general 3x3, row-major
+template <class T> struct SV { V3<T> w, v; };                 // spatial vector
+template <class T> struct Art { S3<T> A; M3<T> B; S3<T> C; };  // [[A, B], [B^T, C]]
+
+template <class T> SPI_INL V3<T> v3(T x, T y, T z) { V3<T> r; r.x = x; r.y = y; r.z = z; return r; }
+template <class T> SPI_INL V3<T> operator+(V3<T> a, V3<T> b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+template <class T> SPI_INL V3<T> operator-(V3<T> a, V3<T> b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+template <class T> SPI_INL V3<T> operator*(T s, V3<T> a) { return v3(s * a.x, s * a.y, s * a.z); }
+template <class T> SPI_INL T dot(V3<T> a, V3<T> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <class T> SPI_INL V3<T> cross(V3<T> a, V3<T> b) {
+  return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+template <class T> SPI_INL V3<T> mul(const S3<T>& S, V3<T> u) {
+  return v3(S.xx * u.x + S.xy * u.y + S.xz * u.z,
+            S.xy * u.x + S.yy * u.y + S.yz * u.z,
+            S.xz * u.x + S.yz * u.y + S.zz * u.z);
+}
+template <class T> SPI_INL V3<T> mul(const M3<T>& M, V3<T> u) {
+  return v3(M.m[0][0] * u.x + M.m[0][1] * u.y + M.m[0][2] * u.z,
+            M.m[1][0] * u.x + M.m[1][1] * u.y + M.m[1][2] * u.z,
+            M.m[2][0] * u.x + M.m[2][1] * u.y + M.m[2][2] * u.z);
+}
+template <class T> SPI_INL V3<T> mulT(const M3<T>& M, V3<T> u) {
+  return v3(M.m[0][0] * u.x + M.m[1][0] * u.y + M.m[2][0] * u.z,
+            M.m[0][1] * u.x + M.m[1][1] * u.y + M.m[2][1] * u.z,
+            M.m[0][2] * u.x + M.m[1][2] * u.y + M.m[2][2] * u.z);
+}
+template <class T> SPI_INL V3<T> row(const M3<T>& M, int i) { return v3(M.m[i][0], M.m[i][1], M.m[i][2]); }
+template <class T> SPI_INL V3<T> col(const S3<T>& S, int j) {
+  return j == 0 ? v3(S.xx, S.xy, S.xz) : (j == 1 ? v3(S.xy, S.yy, S.yz) : v3(S.xz, S.yz, S.zz));
+}
+
+// Active rotation by angle (c, s) about the x (AX = 0) or y (AX = 1) axis, and its transpose.
+template <int AX, class T> SPI_INL V3<T> rot(T c, T s, V3<T> u) {
+  if (AX == 0) return v3(u.x, c * u.y - s * u.z, s * u.y + c * u.z);
+  return v3(c * u.x + s * u.z, u.y, -s * u.x + c * u.z);
+}
+template <int AX, class T> SPI_INL V3<T> rotT(T c, T s, V3<T> u) {
+  if (AX == 0) return v3(u.x, c * u.y + s * u.z, -s * u.y + c * u.z);
+  return v3(c * u.x - s * u.z, u.y, s * u.x + c * u.z);
+}
+// R M R^T for symmetric M and the active plane rotation R about AX.
+template <int AX, class T> SPI_INL S3<T> rot_sym(T c, T s, const S3<T>& M) {
+  S3<T> r;
+  if (AX == 1) {  // plane (x, z): x' = c x + s z, z' = -s x + c z
+    T cc = c * c, ss = s * s, cs = c * s;
+    r.xx = cc * M.xx + T(2) * cs * M.xz + ss * M.zz;
+    r.zz = ss * M.xx - T(2) * cs * M.xz + cc * M.zz;
+    r.xz = cs * (M.zz - M.xx) + (cc - ss) * M.xz;
+    r.xy = c * M.xy + s * M.yz;
+    r.yz = -s * M.xy + c * M.yz;
+    r.yy = M.yy;
+  } else {        // plane (y, z): y' = c y - s z, z' = s y + c z
+    T cc = c * c, ss = s * s, cs = c * s;
+    r.yy = cc * M.yy - T(2) * cs * M.yz + ss * M.zz;
+    r.zz = ss * M.yy + T(2) * cs * M.yz + cc * M.zz;
+    r.yz = cs * (M.yy - M.zz) + (cc - ss) * M.yz;
+    r.xy = c * M.xy - s * M.xz;
+    r.xz = s * M.xy + c * M.xz;
+    r.xx = M.xx;
+  }
+  return r;
+}
+// R B R^T for general B.
+template <int AX, class T> SPI_INL M3<T> rot_gen(T c, T s, const M3<T>& B) {
+  // rows of R B, then columns of (R B) R^T
+  V3<T> r0 = row(B, 0), r1 = row(B, 1), r2 = row(B, 2);
+  V3<T> q0, q1, q2;
+  if (AX == 1) { q0 = c * r0 + s * r2; q1 = r1; q2 = (-s) * r0 + c * r2; }
+  else { q0 = r0; q1 = c * r1 - s * r2; q2 = s * r1 + c * r2; }
+  M3<T> o;
+  V3<T> t0 = rot<AX>(c, s, q0), t1 = rot<AX>(c, s, q1), t2 = rot<AX>(c, s, q2);
+  o.m[0][0] = t0.x; o.m[0][1] = t0.y; o.m[0][2] = t0.z;
+  o.m[1][0] = t1.x; o.m[1][1] = t1.y; o.m[1][2] = t1.z;
+  o.m[2][0] = t2.x; o.m[2][1] = t2.y; o.m[2][2] = t2.z;
+  return o;
+}
+
+// I * v for an articulated inertia.
+template <class T> SPI_INL SV<T> mul(const Art<T>& I, const SV<T>& m) {
+  SV<T> r;
+  r.w = mul(I.A, m.w) + mul(I.B, m.v);
+  r.v = mulT(I.B, m.w) + mul(I.C, m.v);
+  return r;
+}
+// v x* f (force cross product).
+template <class T> SPI_INL SV<T> crf(const SV<T>& v, const SV<T>& f) {
+  SV<T> r;
+  r.w = cross(v.w, f.w) + cross(v.v, f.v);
+  r.v = cross(v.w, f.v);
+  return r;
+}
+// Rigid-body spatial inertia from mass, first moment h = m c and rotational inertia about the origin.
+template <class T> SPI_INL Art<T> rigid(T m, V3<T> h, const S3<T>& Io) {
+  Art<T> I;
+  I.A = Io;
+  I.B.m[0][0] = T(0); I.B.m[0][1] = -h.z; I.B.m[0][2] = h.y;
+  I.B.m[1][0] = h.z;  I.B.m[1][1] = T(0); I.B.m[1][2] = -h.x;
+  I.B.m[2][0] = -h.y; I.B.m[2][1] = h.x;  I.B.m[2][2] = T(0);
+  I.C.xx = m; I.C.yy = m; I.C.zz = m; I.C.xy = T(0); I.C.xz = T(0); I.C.yz = T(0);
+  return I;
+}
+// Rigid-body I*v without forming the 6x6.
+template <class T> SPI_INL SV<T> rigid_mul(T m, V3<T> h, const S3<T>& Io, const SV<T>& v) {
+  SV<T> r;
+  r.w = mul(Io, v.w) + cross(h, v.v);
+  r.v = m * v.v - cross(h, v.w);
+  return r;
+}
+template <class T> SPI_INL void add_to(Art<T>& a, const Art<T>& b) {
+  a.A.xx += b.A.xx; a.A.yy += b.A.yy; a.A.zz += b.A.zz; a.A.xy += b.A.xy; a.A.xz += b.A.xz; a.A.yz += b.A.yz;
+  a.C.xx += b.C.xx; a.C.yy += b.C.yy; a.C.zz += b.C.zz; a.C.xy += b.C.xy; a.C.xz += b.C.xz; a.C.yz += b.C.yz;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) a.B.m[i][j] += b.B.m[i][j];
+}
+// X^T I X for the joint transform X = plucker(R^T, r): rotate by the active joint rotation,
+// then shift by the joint origin r (child origin in parent coordinates).
+template <int AX, class T> SPI_INL Art<T> art_to_parent(const Art<T>& I, T c, T s, V3<T> r) {
+  Art<T> o;
+  S3<T> A1 = rot_sym<AX>(c, s, I.A);
+  M3<T> B1 = rot_gen<AX>(c, s, I.B);
+  S3<T> C1 = rot_sym<AX>(c, s, I.C);
+  // P = skew(r) B1^T: column j = r x (row j of B1)
+  V3<T> p0 = cross(r, row(B1, 0)), p1 = cross(r, row(B1, 1)), p2 = cross(r, row(B1, 2));
+  // Q = skew(r) C1: column j = r x (column j of C1);  skew(r) C1 skew(r): column j = r x (C1 (r x e_j))
+  V3<T> cq0 = cross(r, col(C1, 0)), cq1 = cross(r, col(C1, 1)), cq2 = cross(r, col(C1, 2));
+  V3<T> e0 = v3(T(0), r.z, -r.y), e1 = v3(-r.z, T(0), r.x), e2 = v3(r.y, -r.x, T(0));  // r x e_j
+  V3<T> k0 = cross(r, mul(C1, e0)), k1 = cross(r, mul(C1, e1)), k2 = cross(r, mul(C1, e2));
+  // A' = A1 + P + P^T - skew(r) C1 skew(r)
+  o.A.xx = A1.xx + T(2) * p0.x - k0.x;
+  o.A.yy = A1.yy + T(2) * p1.y - k1.y;
+  o.A.zz = A1.zz + T(2) * p2.z - k2.z;
+  o.A.xy = A1.xy + p1.x + p0.y - k1.x;
+  o.A.xz = A1.xz + p2.x + p0.z - k2.x;
+  o.A.yz = A1.yz + p2.y + p1.z - k2.y;
+  // B' = B1 + skew(r) C1
+  o.B.m[0][0] = B1.m[0][0] + cq0.x; o.B.m[0][1] = B1.m[0][1] + cq1.x; o.B.m[0][2] = B1.m[0][2] + cq2.x;
+  o.B.m[1][0] = B1.m[1][0] + cq0.y; o.B.m[1][1] = B1.m[1][1] + cq1.y; o.B.m[1][2] = B1.m[1][2] + cq2.y;
+  o.B.m[2][0] = B1.m[2][0] + cq0.z; o.B.m[2][1] = B1.m[2][1] + cq1.z; o.B.m[2][2] = B1.m[2][2] + cq2.z;
+  o.C = C1;
+  return o;
+}
+// X^T f: child force to parent coordinates.
+template <int AX, class T> SPI_INL SV<T> force_to_parent(const SV<T>& f, T c, T s, V3<T> r) {
+  SV<T> o;
+  o.v = rot<AX>(c, s, f.v);
+  o.w = rot<AX>(c, s, f.w) + cross(r, o.v);
+  return o;
+}
+// X m: parent motion to child coordinates.
+template <int AX, class T> SPI_INL SV<T> motion_to_child(const SV<T>& m, T c, T s, V3<T> r) {
+  SV<T> o;
+  o.w = rotT<AX>(c, s, m.w);
+  o.v = rotT<AX>(c, s, m.v - cross(r, m.w));
+  return o;
+}
+
+// ---------------------------------------------------------------------------
+// model constants as the kernel sees them (built on the host from spi_robot)
+// ---------------------------------------------------------------------------
+struct DevModel {
+  // per leg body k (0 hip, 1 thigh, 2 calf), component, leg: [k][c][leg] keeps the four
+  // legs' copies of one constant in four consecutive shared-memory banks
+  float org[3][3][4];
+  float m[3][4];
+  float h[3][3][4];
+  float I[3][6][4];   // xx yy zz xy xz yz about the body origin
+  float kp[3][4], kd[3][4], q0[3][4], tlim[3][4], vlim[3][4];
+  float corner[8][3];
+  float foot[3];
+  float gain[3], tanh_a[3];
+  float base_com[3], base_Ic[6];
+  float base_m0, fixed_m, fixed_h[3], fixed_I[6];
+  float foot_r, k, c, ct, mu, ramp_inv, imp_c;
+  float kd_scale, act_scale, act_clip, hip_scale, fric_vel;
+  float dt, g;
+  int decimation, torque_speed, base_contact, inertia_follows_mass;
+};
+
+// ---------------------------------------------------------------------------
+// rollout state
+// ---------------------------------------------------------------------------
+template <class T> struct BaseState {
+  V3<T> p;          // base origin, world
+  T qx, qy, qz, qw; // orientation xyzw
+  SV<T> nu;         // base spatial velocity, base coordinates
+  M3<T> R;          // R(q): base -> world
+};
+template <class T> struct LegState { T q[3], qd[3]; };
+template <class T> struct BaseParams { T m; V3<T> h; S3<T> Io; };   // base rigid inertia (+ fixed links)
+template <class T> struct LegParams { T kps, fc, arm, ts; };        // leg group's motor terms
+template <class T> struct LegOut { Art<T> I; SV<T> p; };            // leg contribution at the base
+template <class T> struct LegWork {                                 // phase A -> phase C
+  SV<T> U[3], cb[3];
+  T invD[3], u[3], c[3], s[3];
+};
+
+template <class T> SPI_INL M3<T> quat_to_R(T x, T y, T z, T w) {
+  M3<T> R;
+  R.m[0][0] = T(1) - T(2) * (y * y + z * z); R.m[0][1] = T(2) * (x * y - z * w); R.m[0][2] = T(2) * (x * z + y * w);
+  R.m[1][0] = T(2) * (x * y + z * w); R.m[1][1] = T(1) - T(2) * (x * x + z * z); R.m[1][2] = T(2) * (y * z - x * w);
+  R.m[2][0] = T(2) * (x * z - y * w); R.m[2][1] = T(2) * (y * z + x * w); R.m[2][2] = T(1) - T(2) * (x * x + y * y);
+  return R;
+}
+
+// theta -> base rigid inertia (base + collapsed fixed links) and leg motor terms.
+template <class T> SPI_INL BaseParams<T> base_params(const DevModel& M, const T* th) {
+  T m = th[0];
+  V3<T> c = v3(T(M.base_com[0]) + th[1], T(M.base_com[1]) + th[2], T(M.base_com[2]) + th[3]);
+  T f = M.inertia_follows_mass ? m / T(M.base_m0) : T(1);
+  S3<T> Ic;
+  Ic.xx = f * T(M.base_Ic[0]) * th[4]; Ic.yy = f * T(M.base_Ic[1]) * th[4]; Ic.zz = f * T(M.base_Ic[2]) * th[4];
+  Ic.xy = f * T(M.base_Ic[3]); Ic.xz = f * T(M.base_Ic[4]); Ic.yz = f * T(M.base_Ic[5]);
+  T cc = dot(c, c);
+  BaseParams<T> b;
+  b.m = m + T(M.fixed_m);
+  b.h = v3(m * c.x + T(M.fixed_h[0]), m * c.y + T(M.fixed_h[1]), m * c.z + T(M.fixed_h[2]));
+  b.Io.xx = Ic.xx + m * (cc - c.x * c.x) + T(M.fixed_I[0]);
+  b.Io.yy = Ic.yy + m * (cc - c.y * c.y) + T(M.fixed_I[1]);
+  b.Io.zz = Ic.zz + m * (cc - c.z * c.z) + T(M.fixed_I[2]);
+  b.Io.xy = Ic.xy - m * c.x * c.y + T(M.fixed_I[3]);
+  b.Io.xz = Ic.xz - m * c.x * c.z + T(M.fixed_I[4]);
+  b.Io.yz = Ic.yz - m * c.y * c.z + T(M.fixed_I[5]);
+  return b;
+}
+template <class T> SPI_INL LegParams<T> leg_params(const T* th, int leg) {
+  const bool rear = leg >= 2;   // selects, not a runtime index: keeps th in registers
+  LegParams<T> p;
+  p.kps = m_sel(rear, th[9], th[5]);
+  p.fc = m_sel(rear, th[10], th[6]);
+  p.arm = m_sel(rear, th[11], th[7]);
+  p.ts = m_sel(rear, th[12], th[8]);
+  return p;
+}
+
+// Penalty contact force (world) on a point at height z with world velocity v; *mimp receives
+// the implicit-damping point mass of the contact (0 without contact).
+template <class T> SPI_INL V3<T> contact_force(const DevModel& M, T radius, T z, V3<T> v, T* mimp) {
+  T pen = radius - z;
+  T s = m_clamp(pen * T(M.ramp_inv), T(0), T(1));
+  T fn = m_sel(pen > T(0), m_fmax(T(0), T(M.k) * pen - T(M.c) * s * v.z), T(0));
+  T vtn = m_sqrt(v.x * v.x + v.y * v.y);
+  T lim = T(M.mu) * fn;
+  T scale = m_sel(T(M.ct) * vtn <= lim, T(M.ct), lim / vtn);
+  *mimp = T(M.dt) * T(M.imp_c) * s;
+  return v3(-scale * v.x, -scale * v.y, fn);
+}
+
+// Spatial inertia of a point mass m at r added to I.
+template <class T> SPI_INL void add_point_mass(Art<T>& I, T m, V3<T> r) {
+  const V3<T> h = m * r;
+  I.A.xx += h.y * r.y + h.z * r.z; I.A.yy += h.x * r.x + h.z * r.z; I.A.zz += h.x * r.x + h.y * r.y;
+  I.A.xy -= h.x * r.y; I.A.xz -= h.x * r.z; I.A.yz -= h.y * r.z;
+  I.B.m[0][1] -= h.z; I.B.m[0][2] += h.y;
+  I.B.m[1][0] += h.z; I.B.m[1][2] -= h.x;
+  I.B.m[2][0] -= h.y; I.B.m[2][1] += h.x;
+  I.C.xx += m; I.C.yy += m; I.C.zz += m;
+}
+
+template <class T> SPI_INL T motor_torque(const DevModel& M, const LegParams<T>& P, int k, int leg,
+                                          T action, T q, T qd) {
+  T a = m_clamp(action, T(-M.act_clip), T(M.act_clip)) * T(M.act_scale);
+  if (k == 0) a = a * T(M.hip_scale);
+  T tau = P.kps * T(M.kp[k][leg]) * (a + T(M.q0[k][leg]) - q) - T(M.kd_scale) * T(M.kd[k][leg]) * qd;
+  T lim = P.ts * T(M.tlim[k][leg]);
+  if (M.torque_speed) lim = lim * m_fmax(T(0), T(1) - m_fabs(qd) / T(M.vlim[k][leg]));
+  tau = m_clamp(tau, -lim, lim) * T(M.gain[k]);
+  if (M.tanh_a[k] > 0.0f) tau = T(M.tanh_a[k]) * m_tanh(tau / T(M.tanh_a[k]));
+  return tau - P.fc * m_tanh(qd / T(M.fric_vel));
+}
+
+template <class T> SPI_INL V3<T> leg_org(const DevModel& M, int k, int leg) {
+  return v3(T(M.org[k][0][leg]), T(M.org[k][1][leg]), T(M.org[k][2][leg]));
+}
+template <class T> SPI_INL Art<T> leg_rigid(const DevModel& M, int k, int leg) {
+  S3<T> Io;
+  Io.xx = T(M.I[k][0][leg]); Io.yy = T(M.I[k][1][leg]); Io.zz = T(M.I[k][2][leg]);
+  Io.xy = T(M.I[k][3][leg]); Io.xz = T(M.I[k][4][leg]); Io.yz = T(M.I[k][5][leg]);
+  return rigid(T(M.m[k][leg]), v3(T(M.h[k][0][leg]), T(M.h[k][1][leg]), T(M.h[k][2][leg])), Io);
+}
+template <class T> SPI_INL SV<T> leg_bias(const DevModel& M, int k, int leg, const SV<T>& v) {
+  S3<T> Io;
+  Io.xx = T(M.I[k][0][leg]); Io.yy = T(M.I[k][1][leg]); Io.zz = T(M.I[k][2][leg]);
+  Io.xy = T(M.I[k][3][leg]); Io.xz = T(M.I[k][4][leg]); Io.yz = T(M.I[k][5][leg]);
+  V3<T> h = v3(T(M.h[k][0][leg]), T(M.h[k][1][leg]), T(M.h[k][2][leg]));
+  return crf(v, rigid_mul(T(M.m[k][leg]), h, Io, v));
+}
+
+// c = v x (S qd) for a revolute joint about axis AX.
+template <int AX, class T> SPI_INL SV<T> vel_product(const SV<T>& v, T qd) {
+  SV<T> c;
+  if (AX == 0) { c.w = v3(T(0), v.w.z * qd, -v.w.y * qd); c.v = v3(T(0), v.v.z * qd, -v.v.y * qd); }
+  else { c.w = v3(-v.w.z * qd, T(0), v.w.x * qd); c.v = v3(-v.v.z * qd, T(0), v.v.x * qd); }
+  return c;
+}
+
+// One ABA backward step of joint k (axis AX): project out the joint, move to the parent.
+template <int AX, class T> SPI_INL void aba_back(Art<T>& IA, SV<T>& pA, const SV<T>& cb, T tau, T arm,
+                                                 T c, T s, V3<T> r, LegWork<T>& W, int k,
+                                                 Art<T>* Iout, SV<T>* pout) {
+  SV<T> U;
+  U.w = col(IA.A, AX);
+  U.v = row(IA.B, AX);
+  T D = (AX == 0 ? IA.A.xx : IA.A.yy) + arm;
+  T invD = T(1) / D;
+  T u = tau - (AX == 0 ? pA.w.x : pA.w.y);
+  // Ia = IA - U U^T / D
+  Art<T> Ia = IA;
+  V3<T> Uw = invD * U.w, Uv = invD * U.v;
+  Ia.A.xx -= Uw.x * U.w.x; Ia.A.yy -= Uw.y * U.w.y; Ia.A.zz -= Uw.z * U.w.z;
+  Ia.A.xy -= Uw.x * U.w.y; Ia.A.xz -= Uw.x * U.w.z; Ia.A.yz -= Uw.y * U.w.z;
+  Ia.B.m[0][0] -= Uw.x * U.v.x; Ia.B.m[0][1] -= Uw.x * U.v.y; Ia.B.m[0][2] -= Uw.x * U.v.z;
+  Ia.B.m[1][0] -= Uw.y * U.v.x; Ia.B.m[1][1] -= Uw.y * U.v.y; Ia.B.m[1][2] -= Uw.y * U.v.z;
+  Ia.B.m[2][0] -= Uw.z * U.v.x; Ia.B.m[2][1] -= Uw.z * U.v.y; Ia.B.m[2][2] -= Uw.z * U.v.z;
+  Ia.C.xx -= Uv.x * U.v.x; Ia.C.yy -= Uv.y * U.v.y; Ia.C.zz -= Uv.z * U.v.z;
+  Ia.C.xy -= Uv.x * U.v.y; Ia.C.xz -= Uv.x * U.v.z; Ia.C.yz -= Uv.y * U.v.z;
+  // pa = pA + Ia c + U u / D
+  SV<T> pa = mul(Ia, cb);
+  T uD = u * invD;
+  pa.w = pA.w + pa.w + uD * U.w;
+  pa.v = pA.v + pa.v + uD * U.v;
+  W.U[k] = U; W.invD[k] = invD; W.u[k] = u;
+  *Iout = art_to_parent<AX>(Ia, c, s, r);
+  *pout = force_to_parent<AX>(pa, c, s, r);
+}
+
+// ---------------------------------------------------------------------------
+// Phase A: everything of one leg (and two base corners) up to its base contribution.
+// ---------------------------------------------------------------------------
+template <class T>
+SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
+                          const LegParams<T>& P, const T act[3], LegWork<T>& W) {
+  T tau[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    tau[k] = motor_torque(M, P, k, leg, act[k], L.q[k], L.qd[k]);
+    m_sincos(L.q[k], &W.s[k], &W.c[k]);
+  }
+  V3<T> r0 = leg_org<T>(M, 0, leg), r1 = leg_org<T>(M, 1, leg), r2 = leg_org<T>(M, 2, leg);
+  // body velocities (body coordinates) and velocity-product accelerations
+  SV<T> v0 = motion_to_child<0>(B.nu, W.c[0], W.s[0], r0); v0.w.x = v0.w.x + L.qd[0];
+  SV<T> v1 = motion_to_child<1>(v0, W.c[1], W.s[1], r1);   v1.w.y = v1.w.y + L.qd[1];
+  SV<T> v2 = motion_to_child<1>(v1, W.c[2], W.s[2], r2);   v2.w.y = v2.w.y + L.qd[2];
+  W.cb[0] = vel_product<0>(v0, L.qd[0]);
+  W.cb[1] = vel_product<1>(v1, L.qd[1]);
+  W.cb[2] = vel_product<1>(v2, L.qd[2]);
+  // foot: position and velocity, calf -> thigh -> hip -> base -> world
+  V3<T> fc = v3(T(M.foot[0]), T(M.foot[1]), T(M.foot[2]));
+  V3<T> vf = v2.v + cross(v2.w, fc);
+  V3<T> pf = rot<1>(W.c[2], W.s[2], fc) + r2;
+  vf = rot<1>(W.c[2], W.s[2], vf);
+  pf = rot<1>(W.c[1], W.s[1], pf) + r1;
+  vf = rot<1>(W.c[1], W.s[1], vf);
+  pf = rot<0>(W.c[0], W.s[0], pf) + r0;
+  vf = rot<0>(W.c[0], W.s[0], vf);
+  T mimp;
+  V3<T> F = contact_force(M, T(M.foot_r), B.p.z + dot(row(B.R, 2), pf), mul(B.R, vf), &mimp);
+  // the implicit point mass acts on the true acceleration while the ABA runs in the
+  // gravity-shifted frame: its share of the shift enters as a force mimp*g upwards
+  F.z = F.z + mimp * T(M.g);
+  V3<T> Fc = mulT(B.R, F);
+  Fc = rotT<0>(W.c[0], W.s[0], Fc);
+  Fc = rotT<1>(W.c[1], W.s[1], Fc);
+  Fc = rotT<1>(W.c[2], W.s[2], Fc);
+  // ABA backward pass: calf -> thigh -> hip -> base
+  Art<T> IA = leg_rigid<T>(M, 2, leg);
+  add_point_mass(IA, mimp, fc);
+  SV<T> pA = leg_bias(M, 2, leg, v2);
+  pA.w = pA.w - cross(fc, Fc);
+  pA.v = pA.v - Fc;
+  Art<T> Ip; SV<T> pp;
+  aba_back<1>(IA, pA, W.cb[2], tau[2], P.arm, W.c[2], W.s[2], r2, W, 2, &Ip, &pp);
+  IA = leg_rigid<T>(M, 1, leg); add_to(IA, Ip);
+  pA = leg_bias(M, 1, leg, v1); pA.w = pA.w + pp.w; pA.v = pA.v + pp.v;
+  aba_back<1>(IA, pA, W.cb[1], tau[1], P.arm, W.c[1], W.s[1], r1, W, 1, &Ip, &pp);
+  IA = leg_rigid<T>(M, 0, leg); add_to(IA, Ip);
+  pA = leg_bias(M, 0, leg, v0); pA.w = pA.w + pp.w; pA.v = pA.v + pp.v;
+  LegOut<T> out;
+  aba_back<0>(IA, pA, W.cb[0], tau[0], P.arm, W.c[0], W.s[0], r0, W, 0, &out.I, &out.p);
+  // two of the eight base-box corners
+  if (M.base_contact) {
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const float* cc = M.corner[2 * leg + j];
+      V3<T> rc = v3(T(cc[0]), T(cc[1]), T(cc[2]));
+      V3<T> vc = B.nu.v + cross(B.nu.w, rc);
+      T mc;
+      V3<T> Fw = contact_force(M, T(0), B.p.z + dot(row(B.R, 2), rc), mul(B.R, vc), &mc);
+      Fw.z = Fw.z + mc * T(M.g);
+      V3<T> Fb = mulT(B.R, Fw);
+      out.p.w = out.p.w - cross(rc, Fb);
+      out.p.v = out.p.v - Fb;
+      add_point_mass(out.I, mc, rc);
+    }
+  }
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+// Phase B: base solve and base integration. `sum` is the sum of the four LegOut.
+// Returns the base acceleration with gravity removed (the frame the legs' forward pass uses).
+// ---------------------------------------------------------------------------
+template <class T>
+SPI_INL SV<T> phase_b(const DevModel& M, const BaseParams<T>& bp, const LegOut<T>& sum, BaseState<T>& B) {
+  Art<T> IA = rigid(bp.m, bp.h, bp.Io);
+  add_to(IA, sum.I);
+  SV<T> pA = crf(B.nu, rigid_mul(bp.m, bp.h, bp.Io, B.nu));
+  pA.w = pA.w + sum.p.w;
+  pA.v = pA.v + sum.p.v;
+  // 6x6 symmetric matrix in (w; v) order, Cholesky L L^T, solve IA a = -pA
+  T Mx[6][6];
+  Mx[0][0] = IA.A.xx; Mx[1][1] = IA.A.yy; Mx[2][2] = IA.A.zz;
+  Mx[1][0] = IA.A.xy; Mx[2][0] = IA.A.xz; Mx[2][1] = IA.A.yz;
+  Mx[3][3] = IA.C.xx; Mx[4][4] = IA.C.yy; Mx[5][5] = IA.C.zz;
+  Mx[4][3] = IA.C.xy; Mx[5][3] = IA.C.xz; Mx[5][4] = IA.C.yz;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) Mx[3 + j][i] = IA.B.m[i][j];   // lower block = B^T
+  T rhs[6] = {-pA.w.x, -pA.w.y, -pA.w.z, -pA.v.x, -pA.v.y, -pA.v.z};
+  T invL[6];
+#pragma unroll
+  for (int j = 0; j < 6; ++j) {
+    T d = Mx[j][j];
+#pragma unroll
+    for (int k = 0; k < j; ++k) d = d - Mx[j][k] * Mx[j][k];
+    T inv = T(1) / m_sqrt(d);
+    invL[j] = inv;
+#pragma unroll
+    for (int i = j + 1; i < 6; ++i) {
+      T a = Mx[i][j];
+#pragma unroll
+      for (int k = 0; k < j; ++k) a = a - Mx[i][k] * Mx[j][k];
+      Mx[i][j] = a * inv;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    T a = rhs[i];
+#pragma unroll
+    for (int k = 0; k < i; ++k) a = a - Mx[i][k] * rhs[k];
+    rhs[i] = a * invL[i];
+  }
+#pragma unroll
+  for (int i = 5; i >= 0; --i) {
+    T a = rhs[i];
+#pragma unroll
+    for (int k = i + 1; k < 6; ++k) a = a - Mx[k][i] * rhs[k];
+    rhs[i] = a * invL[i];
+  }
+  SV<T> a0;
+  a0.w = v3(rhs[0], rhs[1], rhs[2]);
+  a0.v = v3(rhs[3], rhs[4], rhs[5]);
+  // integrate: true acceleration adds gravity expressed in base coordinates
+  T dt = T(M.dt), g = T(M.g);
+  B.nu.w = B.nu.w + dt * a0.w;
+  B.nu.v = B.nu.v + dt * (a0.v - g * row(B.R, 2));
+  T hx = T(0.5) * dt;
+  V3<T> w = B.nu.w;
+  T nx = B.qx + hx * (B.qw * w.x + (B.qy * w.z - B.qz * w.y));
+  T ny = B.qy + hx * (B.qw * w.y + (B.qz * w.x - B.qx * w.z));
+  T nz = B.qz + hx * (B.qw * w.z + (B.qx * w.y - B.qy * w.x));
+  T nw = B.qw - hx * (B.qx * w.x + B.qy * w.y + B.qz * w.z);
+  T inv = T(1) / m_sqrt(nx * nx + ny * ny + nz * nz + nw * nw);
+  B.qx = nx * inv; B.qy = ny * inv; B.qz = nz * inv; B.qw = nw * inv;
+  B.R = quat_to_R(B.qx, B.qy, B.qz, B.qw);
+  B.p = B.p + dt * mul(B.R, B.nu.v);
+  return a0;
+}
+
+// ---------------------------------------------------------------------------
+// Phase C: forward pass of one leg from the base acceleration, then joint integration.
+// ---------------------------------------------------------------------------
+template <class T>
+SPI_INL void phase_c(const DevModel& M, int leg, const SV<T>& a0, const LegWork<T>& W, LegState<T>& L) {
+  T qdd[3];
+  SV<T> a = motion_to_child<0>(a0, W.c[0], W.s[0], leg_org<T>(M, 0, leg));
+  a.w = a.w + W.cb[0].w; a.v = a.v + W.cb[0].v;
+  qdd[0] = (W.u[0] - dot(W.U[0].w, a.w) - dot(W.U[0].v, a.v)) * W.invD[0];
+  a.w.x = a.w.x + qdd[0];
+  a = motion_to_child<1>(a, W.c[1], W.s[1], leg_org<T>(M, 1, leg));
+  a.w = a.w + W.cb[1].w; a.v = a.v + W.cb[1].v;
+  qdd[1] = (W.u[1] - dot(W.U[1].w, a.w) - dot(W.U[1].v, a.v)) * W.invD[1];
+  a.w.y = a.w.y + qdd[1];
+  a = motion_to_child<1>(a, W.c[2], W.s[2], leg_org<T>(M, 2, leg));
+  a.w = a.w + W.cb[2].w; a.v = a.v + W.cb[2].v;
+  qdd[2] = (W.u[2] - dot(W.U[2].w, a.w) - dot(W.U[2].v, a.v)) * W.invD[2];
+  T dt = T(M.dt);
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    L.qd[k] = L.qd[k] + dt * qdd[k];
+    L.q[k] = L.q[k] + dt * L.qd[k];
+  }
+}
+
+// Window start: world-frame root state -> body-frame velocity.
+template <class T> SPI_INL void base_from_world(BaseState<T>& B, const T* s13) {
+  B.p = v3(s13[0], s13[1], s13[2]);
+  B.qx = s13[3]; B.qy = s13[4]; B.qz = s13[5]; B.qw = s13[6];
+  B.R = quat_to_R(B.qx, B.qy, B.qz, B.qw);
+  B.nu.v = mulT(B.R, v3(s13[7], s13[8], s13[9]));
+  B.nu.w = mulT(B.R, v3(s13[10], s13[11], s13[12]));
+}
+template <class T> SPI_INL void base_to_world(const BaseState<T>& B, T* s13) {
+  s13[0] = B.p.x; s13[1] = B.p.y; s13[2] = B.p.z;
+  s13[3] = B.qx; s13[4] = B.qy; s13[5] = B.qz; s13[6] = B.qw;
+  V3<T> v = mul(B.R, B.nu.v), w = mul(B.R, B.nu.w);
+  s13[7] = v.x; s13[8] = v.y; s13[9] = v.z;
+  s13[10] = w.x; s13[11] = w.y; s13[12] = w.z;
+}
+
+}  // namespace spi

@@ -23,3 +23,25 @@ def golden():
     def _load(name):
         return np.load(GOLDEN / f"{name}.npz", allow_pickle=False)
     return _load
+
+
+def pytest_collection_modifyitems(config, items):
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        return
+    skip = pytest.mark.skip(reason="no CUDA device")
+    for item in items:
+        if "gpu" in item.keywords:
+            item.add_marker(skip)
+
+
+@pytest.fixture(scope="session")
+def built():
+    """Build the native libraries once per session (nvcc + g++)."""
+    from spi_gb300 import _build
+    _build.build()
+    return _build
