@@ -120,12 +120,20 @@ int spi_cem_run(spi_engine* e, int iterations, int use_graph) {
     return SPI_OK;
   }
   if (!e->graph_exec) {
-    if (!e->stream) return set_error(SPI_EINVAL, "spi_cem_run: graph capture needs a non-default stream");
+    // capture one iteration on a private stream (the engine stream may be the legacy
+    // default stream, which cannot be captured), replay it on the engine stream
+    if (!e->capture_stream) {
+      cudaError_t ce = cudaStreamCreateWithFlags(&e->capture_stream, cudaStreamNonBlocking);
+      if (ce != cudaSuccess) return cuda_error(ce, "spi_cem_run: capture stream");
+    }
     cudaGraph_t g = nullptr;
+    cudaStream_t user = e->stream;
+    e->stream = e->capture_stream;
     cudaError_t ce = cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal);
-    if (ce != cudaSuccess) return cuda_error(ce, "spi_cem_run: begin capture");
+    if (ce != cudaSuccess) { e->stream = user; return cuda_error(ce, "spi_cem_run: begin capture"); }
     int rc = cem_step_impl(e);
     ce = cudaStreamEndCapture(e->stream, &g);
+    e->stream = user;
     if (rc) { if (g) cudaGraphDestroy(g); return rc; }
     if (ce != cudaSuccess) return cuda_error(ce, "spi_cem_run: end capture");
     ce = cudaGraphInstantiate(&e->graph_exec, g, 0);

@@ -111,6 +111,7 @@ int spi_create(const spi_robot* robot, spi_engine** out) {
 int spi_destroy(spi_engine* e) {
   if (!e) return SPI_OK;
   if (e->graph_exec) cudaGraphExecDestroy(e->graph_exec);
+  if (e->capture_stream) cudaStreamDestroy(e->capture_stream);
   if (e->d_model) cudaFree(e->d_model);
   delete e;
   return SPI_OK;

@@ -25,6 +25,7 @@ struct spi_engine {
   spi::DeviceBuf cem;                      // one CemState
   bool cem_ready = false;
   cudaGraphExec_t graph_exec = nullptr;
+  cudaStream_t capture_stream = nullptr;   // graphs are captured here, replayed on `stream`
 };
 
 namespace spi {
