@@ -76,9 +76,10 @@ def n_elite(n_samples, elite_frac=0.1):
 
 
 def elite_order(cost):
-    """Indices sorted by (cost ascending, index ascending); NaN sorts last."""
-    c = np.where(np.isnan(cost), np.inf, np.asarray(cost, dtype=np.float64))
-    return np.lexsort((np.arange(c.shape[0]), c))
+    """Indices sorted by (cost ascending, index ascending); NaN sorts after +inf."""
+    c = np.asarray(cost, dtype=np.float64)
+    nan = np.isnan(c)
+    return np.lexsort((np.arange(c.shape[0]), np.where(nan, np.inf, c), nan))
 
 
 def refit(theta, cost, ne, mu_prev, cov_prev, alpha, min_std):

@@ -119,3 +119,9 @@ def test_cem_converges_on_quadratic():
         mu, cov = cem.refit(th, c, cem.n_elite(256), mu, cov, 1.0, 1e-4 * (hi - lo))
         th = cem.sample(mu, cov, lo, hi, 7, 0, it, 256)
     assert np.abs(mu - target).max() < 1e-2
+
+
+def test_elite_order_ties_inf_and_nan():
+    """Same order as the device keys: cost ascending, ties by index, +inf, then NaN."""
+    c = np.array([3.0, np.nan, 1.0, 1.0, 0.0, np.inf, 2.0], dtype=np.float32)
+    assert list(cem.elite_order(c)) == [4, 2, 3, 6, 0, 5, 1]
