@@ -160,6 +160,25 @@ int spi_cem_run(spi_engine* e, int iterations, int use_graph);
 int spi_cem_read(spi_engine* e, double* mu, double* cov, float* best_theta, float* best_cost,
                  int32_t* iteration);
 
+/* ---- evaluation without any device allocation ---------------------------------------
+ * No counterpart in the reference. For callers that must not let a library call cudaMalloc:
+ * a serving process that reserves its HBM budget up front, a host framework that owns every
+ * device allocation, or a loop where cudaMalloc's implicit device synchronisation would stall
+ * other streams. Same dynamics and costs as spi_load_windows + spi_set_theta + spi_run +
+ * spi_read_costs, but the caller's row-layout device buffers are read directly (init and
+ * target [W][37], actions [W][H][12], weight [W] or NULL, theta [N][13]; outputs comp [N][9]
+ * and cost [N], either may be NULL), the model is passed by value to the kernel, and the
+ * per-(theta, 8-window group) partial sums use a fixed file-scope device array that every
+ * GPU loading the library keeps until exit: N * ceil(W / 8) <= SPI_NOALLOC_MAX_GROUPS, larger
+ * requests fail with SPI_EINVAL. All calls share that array, so calls that overlap on the GPU
+ * race; serialise them. The first call on a device looks up the array's address on that
+ * device; make it before any stream capture. Asynchronous on `stream` (a cudaStream_t). */
+#define SPI_NOALLOC_MAX_GROUPS 65536
+int spi_eval_windows_noalloc(const spi_robot* robot, const float* init, const float* actions,
+                             const float* target, const float* weight, int W, int H, float norm,
+                             const float* theta, int N, int cost_mode, const float* sq_weights,
+                             float* comp, float* cost, void* stream);
+
 /* Upper bound of the FP32 throughput of this GPU, measured by an FMA loop [FLOP/s]. */
 int spi_probe_fp32_peak(double* flops_per_s);
 

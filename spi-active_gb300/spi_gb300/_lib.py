@@ -41,6 +41,9 @@ ENGINE_API = {
     "spi_sync": (c_int, [c_void_p, POINTER(c_int64)]),
     "spi_read_theta": (c_int, [c_void_p, c_void_p]),
     "spi_probe_fp32_peak": (c_int, [POINTER(c_double)]),
+    "spi_eval_windows_noalloc": (c_int, [POINTER(SpiRobot), c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int,
+                                         c_float, c_void_p, c_int, c_int, POINTER(c_float), c_void_p, c_void_p,
+                                         c_void_p]),
 }
 
 
