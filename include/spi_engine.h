@@ -113,6 +113,10 @@ int spi_set_theta(spi_engine* e, const float* theta, int N);
  * mode 1 = weighted squared error with sq_weights[6] (pos, quat, linvel, angvel, q, qd). */
 int spi_set_cost(spi_engine* e, int mode, const float* sq_weights);
 
+/* Rollout-kernel variant: the register allocator targets min_blocks CTAs of 128 threads per
+ * SM (3: 168 registers, no spills; 4: 128 registers; 5: 96 registers). Same results. */
+int spi_set_kernel_config(spi_engine* e, int min_blocks);
+
 /* Roll every (theta, window) pair H control steps and reduce the windowed cost. Async. */
 int spi_run(spi_engine* e);
 /* Same, also writing every control step's state to trace, device [N][W][H][37]. */
@@ -159,6 +163,76 @@ int spi_cem_run(spi_engine* e, int iterations, int use_graph);
  * cov [P][P], best theta [13] and cost over all iterations, iterations done. */
 int spi_cem_read(spi_engine* e, double* mu, double* cov, float* best_theta, float* best_cost,
                  int32_t* iteration);
+
+/* ---- sensitivities and Fisher information (active excitation design) ------------------
+ * Replaces the finite-difference Fisher proxy of the reference
+ * (spigym/envs/sysid/active_sysid_openloop.py:402-426, main env vs aux envs with theta + 0.1,
+ * trace(J^T J)) with exact forward-mode derivatives of the rollout.
+ * spi_sensitivity: J[n][w][i][k] = d s_H[i] / d theta[param_ids[k]] of window w (the loaded
+ * windows) for theta sample n (device [N][13]); J device [N][W][37][K]; xH device
+ * [N][W][37] final states or NULL. K <= 13. Asynchronous on the engine stream.
+ * spi_fisher: F[n] = sum_w J_w^T diag(state_weight) J_w (device [N][K][K], FP32
+ * accumulation), logdet[n] = log det(F[n] + eps I) and trace[n] = trace(F[n]) in FP64
+ * (device [N] each, may be NULL). */
+int spi_sensitivity(spi_engine* e, const float* theta, int N, const int32_t* param_ids, int K, float* J,
+                    float* xH);
+int spi_fisher(const float* J, int N, int W, int K, const float* state_weight, double eps, float* F,
+               double* logdet, double* trace, void* stream);
+
+/* ---- continuous-batching identification server ------------------------------------------
+ * Many sysid jobs of uneven population, window count, horizon and parameter dimension share
+ * the GPU. Each job is one CEM identification (the work of scripts/mass_opt.py per dataset);
+ * jobs are admitted into slots against an HBM budget as they arrive, every tick advances
+ * every active job by one CEM iteration in one persistent rollout launch (work items are
+ * (job, theta, 8-window group), claimed longest-horizon first), and finished jobs free their
+ * slot and memory for the next arrivals. One tick is captured once as a CUDA graph. A job's
+ * results do not depend on the other jobs in the mix (each work item runs the same code on
+ * the same inputs wherever it is scheduled). No counterpart in the reference, which runs
+ * one job at a time. */
+typedef struct spi_server spi_server;
+
+typedef struct spi_job {
+    const float* init;       /* device [W][37] */
+    const float* actions;    /* device [W][H][12] */
+    const float* target;     /* device [W][37] */
+    const float* weight;     /* device [W] or NULL */
+    int32_t W, H;
+    float norm;              /* <= 0: W */
+    int32_t iterations;      /* CEM iterations to run */
+    spi_cem_config cem;      /* population, identified slots, priors, seed */
+} spi_job;
+
+typedef struct spi_job_result {
+    int32_t job_id;          /* spi_cem_config.job_id of the job */
+    int32_t iterations;
+    float best_cost;
+    float best_theta[SPI_THETA_DIM];
+    double mu[SPI_THETA_DIM];            /* mean over the identified parameters (first `dim`) */
+    int32_t dim;
+    int32_t status;          /* 0 ok, 1 covariance needed the std floor at some refit */
+} spi_job_result;
+
+/* max_slots concurrent jobs, each with at most max_samples theta; hbm_budget_bytes caps the
+ * device memory of admitted jobs (spi_server_job_bytes gives a job's share). */
+int spi_server_create(const spi_robot* robot, int max_slots, int max_samples, size_t hbm_budget_bytes,
+                      spi_server** out);
+int spi_server_destroy(spi_server* s);
+int spi_server_set_stream(spi_server* s, void* stream);
+int spi_server_set_cost(spi_server* s, int mode, const float* sq_weights);
+size_t spi_server_job_bytes(const spi_job* job);
+/* Admit a job: SPI_OK and its slot, or SPI_EBUDGET when no slot or memory is free now. The
+ * window buffers are copied; the caller may free them once the call returns. */
+int spi_server_submit(spi_server* s, const spi_job* job, int32_t* slot);
+/* One CEM iteration for every active job (asynchronous). */
+int spi_server_tick(spi_server* s);
+/* Collect up to `max` finished jobs (host results); *n_done receives how many. */
+int spi_server_poll(spi_server* s, spi_job_result* results, int max, int32_t* n_done);
+/* Block until every tick and result copy enqueued so far has finished. */
+int spi_server_wait(spi_server* s);
+/* Active job count and free budget. */
+int spi_server_stats(spi_server* s, int32_t* active, size_t* bytes_free);
+/* Persistent-grid shape: CTAs per SM (0 = occupancy maximum) and work items claimed per atomic. */
+int spi_server_config(spi_server* s, int ctas_per_sm, int items_per_claim);
 
 /* ---- evaluation without any device allocation ---------------------------------------
  * No counterpart in the reference. For callers that must not let a library call cudaMalloc:

@@ -12,8 +12,11 @@ using namespace spi;
 namespace {
 
 int cem_sample_impl(spi_engine* e) {
+  int rc = refresh_after_realloc(e);
+  if (rc) return rc;
+  e->N = e->cem_n;
   CemState* st = (CemState*)e->cem.p;
-  cem_sample_kernel<<<dim3(blocks_for(e->N, 128), 1), 128, 0, e->stream>>>(st, 0, e->theta.f(), nullptr);
+  cem_sample_kernel<<<dim3(blocks_for(e->N, 128), 1), 128, 0, e->stream>>>(st);
   cudaError_t ce = cudaGetLastError();
   return ce == cudaSuccess ? SPI_OK : cuda_error(ce, "cem_sample_kernel");
 }
@@ -21,8 +24,7 @@ int cem_sample_impl(spi_engine* e) {
 int cem_refit_impl(spi_engine* e) {
   int npad = 1;
   while (npad < e->N) npad <<= 1;
-  cem_refit_kernel<<<1, 1024, npad * sizeof(unsigned long long), e->stream>>>(
-      (CemState*)e->cem.p, e->theta.f(), nullptr, e->cost.f(), nullptr);
+  cem_refit_kernel<<<1, 1024, npad * sizeof(unsigned long long), e->stream>>>((CemState*)e->cem.p);
   cudaError_t ce = cudaGetLastError();
   return ce == cudaSuccess ? SPI_OK : cuda_error(ce, "cem_refit_kernel");
 }
@@ -35,6 +37,22 @@ int cem_step_impl(spi_engine* e) {
 }
 
 }  // namespace
+
+int spi::refresh_after_realloc(spi_engine* e) {
+  const unsigned gen = e->theta.generation + e->cost.generation + e->partial.generation + e->comp.generation +
+                       e->init.generation + e->act.generation + e->tgt.generation + e->weight.generation;
+  if (gen == e->seen_generation) return SPI_OK;
+  e->seen_generation = gen;
+  if (e->graph_exec) { cudaGraphExecDestroy(e->graph_exec); e->graph_exec = nullptr; }
+  if (!e->cem_ready) return SPI_OK;
+  float* ptrs[2] = {e->theta.f(), e->cost.f()};
+  CemState* st = (CemState*)e->cem.p;
+  cudaError_t ce = cudaMemcpyAsync(&st->theta, &ptrs[0], sizeof(float*), cudaMemcpyHostToDevice, e->stream);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync((void*)&st->cost, &ptrs[1], sizeof(float*), cudaMemcpyHostToDevice, e->stream);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);   // the host array is on the stack
+  return ce == cudaSuccess ? SPI_OK : cuda_error(ce, "refresh CEM buffer pointers");
+}
 
 extern "C" {
 
@@ -74,6 +92,7 @@ int spi_cem_init(spi_engine* e, const spi_cem_config* c) {
   if (h.n_elite < 2) h.n_elite = 2;
   h.seed = c->seed;
   h.job = c->job_id;
+  h.active = 1;
   cudaError_t ce = cudaFuncSetAttribute(cem_refit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         CEM_MAX_SAMPLES * (int)sizeof(unsigned long long));
   if (ce != cudaSuccess) return cuda_error(ce, "spi_cem_init: refit shared memory");
@@ -84,12 +103,17 @@ int spi_cem_init(spi_engine* e, const spi_cem_config* c) {
   if ((rc = e->partial.reserve((size_t)c->n_samples * G * SPI_N_COMP * 4))) return rc;
   if ((rc = e->comp.reserve((size_t)c->n_samples * SPI_N_COMP * 4))) return rc;
   if ((rc = e->cost.reserve((size_t)c->n_samples * 4))) return rc;
+  h.theta = e->theta.f();
+  h.cost = e->cost.f();
   ce = cudaMemcpyAsync(e->cem.p, &h, sizeof(h), cudaMemcpyHostToDevice, e->stream);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(e->stream);
   if (ce != cudaSuccess) return cuda_error(ce, "spi_cem_init: upload");
   e->N = c->n_samples;
+  e->cem_n = c->n_samples;
   e->cem_ready = true;
   if (e->graph_exec) { cudaGraphExecDestroy(e->graph_exec); e->graph_exec = nullptr; }
+  e->seen_generation = e->theta.generation + e->cost.generation + e->partial.generation + e->comp.generation +
+                       e->init.generation + e->act.generation + e->tgt.generation + e->weight.generation;
   return SPI_OK;
 }
 

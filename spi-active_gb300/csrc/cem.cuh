@@ -39,20 +39,19 @@ __device__ __forceinline__ unsigned long long cost_key(float c, unsigned idx) {
   return ((unsigned long long)o << 32) | idx;
 }
 
-// Draw the population of the current iteration into theta [N][13].
-__global__ void cem_sample_kernel(CemState* __restrict__ st_all, int job_offset, float* __restrict__ theta_base,
-                                  const long long* __restrict__ theta_offsets) {
-  CemState* st = st_all + blockIdx.y;
+// Draw the population of the current iteration into st->theta; one grid row per state.
+static __global__ void cem_sample_kernel(const CemState* __restrict__ st_all) {
+  const CemState* st = st_all + blockIdx.y;
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= st->n_samples) return;
-  float* theta = theta_base + (theta_offsets ? theta_offsets[blockIdx.y] : 0) + (size_t)n * SPI_THETA_DIM;
+  if (!st->active || n >= st->n_samples) return;
+  float* theta = st->theta + (size_t)n * SPI_THETA_DIM;
   const int P = st->dim, it = st->iter;
   const uint32_t k0 = (uint32_t)(st->seed & 0xFFFFFFFFull), k1 = (uint32_t)(st->seed >> 32);
   double z[CEM_MAX_DIM + 3];
 #pragma unroll
   for (int b = 0; b < (CEM_MAX_DIM + 3) / 4; ++b) {
     if (4 * b >= P) break;
-    uint32_t c[4] = {(uint32_t)n, (uint32_t)it, (uint32_t)b, (uint32_t)(st->job + job_offset)};
+    uint32_t c[4] = {(uint32_t)n, (uint32_t)it, (uint32_t)b, (uint32_t)st->job};
     philox4x32_10(c, k0, k1);
     if (it == 0) {
 #pragma unroll
@@ -96,18 +95,15 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
-// One CTA (1024 threads) per job: elite select + mean / covariance + Cholesky.
-__global__ void __launch_bounds__(1024) cem_refit_kernel(CemState* __restrict__ st_all,
-                                                         const float* __restrict__ theta_base,
-                                                         const long long* __restrict__ theta_offsets,
-                                                         const float* __restrict__ cost_base,
-                                                         const long long* __restrict__ cost_offsets) {
+// One CTA (1024 threads) per state: elite select + mean / covariance + Cholesky.
+static __global__ void __launch_bounds__(1024) cem_refit_kernel(CemState* __restrict__ st_all) {
   extern __shared__ unsigned long long keys[];
   __shared__ double s_mu[CEM_MAX_DIM];
   __shared__ double s_cov[CEM_MAX_DIM * CEM_MAX_DIM];
   CemState* st = st_all + blockIdx.x;
-  const float* theta = theta_base + (theta_offsets ? theta_offsets[blockIdx.x] : 0);
-  const float* cost = cost_base + (cost_offsets ? cost_offsets[blockIdx.x] : 0);
+  if (!st->active) return;   // uniform per CTA
+  const float* theta = st->theta;
+  const float* cost = st->cost;
   const int N = st->n_samples, P = st->dim, ne = st->n_elite;
   int npad = 1;
   while (npad < N) npad <<= 1;

@@ -19,7 +19,10 @@ struct CemState {
   float best_cost;
   int param_ids[CEM_MAX_DIM];
   int dim, n_samples, n_elite, iter, job, status;
+  int active;              // 0: slot unused (kernels skip it)
   unsigned long long seed;
+  float* theta;            // population [n_samples][13] this state samples into
+  const float* cost;       // costs [n_samples] its refit reads
 };
 
 }  // namespace spi

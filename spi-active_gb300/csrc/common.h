@@ -17,6 +17,7 @@ int cuda_error(cudaError_t e, const char* what);
 struct DeviceBuf {
   void* p = nullptr;
   size_t cap = 0;
+  unsigned generation = 0;   // bumped whenever the allocation moves
   DeviceBuf() = default;
   DeviceBuf(const DeviceBuf&) = delete;
   DeviceBuf& operator=(const DeviceBuf&) = delete;
@@ -30,6 +31,7 @@ struct DeviceBuf {
       return set_error(SPI_ENOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
     }
     cap = bytes;
+    ++generation;
     return SPI_OK;
   }
   float* f() const { return static_cast<float*>(p); }

@@ -45,11 +45,23 @@ namespace spi {
 // ---------------------------------------------------------------------------
 SPI_INL float m_sqrt(float x) { return sqrtf(x); }
 SPI_INL double m_sqrt(double x) { return sqrt(x); }
-SPI_INL float m_tanh(float x) { return tanhf(x); }
+// Device FP32: tanh from one MUFU exponential, 1 - 2/(e^{2x} + 1) (absolute error ~1e-7; the
+// exponent is clamped so e^{2x} stays finite).
+SPI_INL float m_tanh(float x) {
+#if defined(__CUDA_ARCH__)
+  const float e = __expf(2.0f * fminf(fmaxf(x, -15.0f), 15.0f));
+  return 1.0f - __fdividef(2.0f, e + 1.0f);
+#else
+  return tanhf(x);
+#endif
+}
 SPI_INL double m_tanh(double x) { return tanh(x); }
+// Device FP32: reduce to [-pi, pi] (joint angles stay within a few radians), then the MUFU
+// sine / cosine, whose absolute error there is ~2^-21.
 SPI_INL void m_sincos(float x, float* s, float* c) {
 #if defined(__CUDA_ARCH__)
-  sincosf(x, s, c);
+  const float r = fmaf(-6.28318530717958648f, rintf(x * 0.159154943091895336f), x);
+  __sincosf(r, s, c);
 #else
   *s = sinf(x); *c = cosf(x);
 #endif

@@ -61,16 +61,23 @@ int spi::run_impl(spi_engine* e, float* trace) {
   if (rc) return rc;
   rc = e->cost.reserve((size_t)e->N * sizeof(float));
   if (rc) return rc;
+  if ((rc = refresh_after_realloc(e))) return rc;
   WinView win{e->init.f(), e->act.f(), e->tgt.f(), e->weight.f(), e->W, e->H};
   const long long warps = (long long)e->N * G;
   const unsigned grid = blocks_for(warps, 4);
   unsigned long long* bad = (unsigned long long*)e->bad.p;
   if (trace)
-    rollout_kernel<true><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
-                                                      e->partial.f(), trace, bad);
+    rollout_kernel<true, 3><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
+                                                         e->partial.f(), trace, bad);
+  else if (e->min_blocks == 4)
+    rollout_kernel<false, 4><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
+                                                          e->partial.f(), nullptr, bad);
+  else if (e->min_blocks == 5)
+    rollout_kernel<false, 5><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
+                                                          e->partial.f(), nullptr, bad);
   else
-    rollout_kernel<false><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
-                                                       e->partial.f(), nullptr, bad);
+    rollout_kernel<false, 3><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
+                                                          e->partial.f(), nullptr, bad);
   cudaError_t ce = cudaGetLastError();
   if (ce != cudaSuccess) return cuda_error(ce, "rollout_kernel launch");
   const float* w = e->sq_w;
@@ -133,6 +140,7 @@ int spi_load_windows(spi_engine* e, const float* init, const float* actions, con
   if ((rc = e->tgt.reserve((size_t)W * SPI_STATE_DIM * 4))) return rc;
   if ((rc = e->act.reserve((size_t)W * H * 12 * 4))) return rc;
   if ((rc = e->weight.reserve((size_t)W * 4))) return rc;
+  if ((rc = refresh_after_realloc(e))) return rc;
   const long long ns = (long long)W * SPI_STATE_DIM;
   rows_to_soa<<<blocks_for(ns, 256), 256, 0, e->stream>>>(init, e->init.f(), W, SPI_STATE_DIM);
   rows_to_soa<<<blocks_for(ns, 256), 256, 0, e->stream>>>(target, e->tgt.f(), W, SPI_STATE_DIM);
@@ -147,6 +155,8 @@ int spi_load_windows(spi_engine* e, const float* init, const float* actions, con
   e->H = H;
   e->norm = norm > 0.f ? norm : (float)W;
   e->ran = false;
+  // a captured CEM iteration bakes in W, H and norm: capture again on next use
+  if (e->graph_exec) { cudaGraphExecDestroy(e->graph_exec); e->graph_exec = nullptr; }
   return SPI_OK;
 }
 
@@ -155,6 +165,7 @@ int spi_set_theta(spi_engine* e, const float* theta, int N) {
   if (N <= 0) return set_error(SPI_EINVAL, "spi_set_theta: N=%d must be > 0", N);
   int rc = e->theta.reserve((size_t)N * SPI_THETA_DIM * 4);
   if (rc) return rc;
+  if ((rc = refresh_after_realloc(e))) return rc;
   cudaError_t ce = cudaMemcpyAsync(e->theta.p, theta, (size_t)N * SPI_THETA_DIM * 4,
                                    cudaMemcpyDeviceToDevice, e->stream);
   if (ce != cudaSuccess) return cuda_error(ce, "spi_set_theta");
@@ -163,11 +174,21 @@ int spi_set_theta(spi_engine* e, const float* theta, int N) {
   return SPI_OK;
 }
 
+int spi_set_kernel_config(spi_engine* e, int min_blocks) {
+  if (!e) return set_error(SPI_EINVAL, "null engine");
+  if (min_blocks < 3 || min_blocks > 5)
+    return set_error(SPI_EINVAL, "spi_set_kernel_config: min_blocks %d outside [3, 5]", min_blocks);
+  e->min_blocks = min_blocks;
+  if (e->graph_exec) { cudaGraphExecDestroy(e->graph_exec); e->graph_exec = nullptr; }
+  return SPI_OK;
+}
+
 int spi_set_cost(spi_engine* e, int mode, const float* sq_weights) {
   if (!e) return set_error(SPI_EINVAL, "null engine");
   if (mode != 0 && mode != 1) return set_error(SPI_EINVAL, "spi_set_cost: mode %d not 0/1", mode);
   e->cost_mode = mode;
   if (sq_weights) memcpy(e->sq_w, sq_weights, sizeof(e->sq_w));
+  if (e->graph_exec) { cudaGraphExecDestroy(e->graph_exec); e->graph_exec = nullptr; }
   return SPI_OK;
 }
 

@@ -155,9 +155,11 @@ __device__ __forceinline__ void rollout_group(const DevModel& M, const WinView& 
   }
 }
 
-// One warp per (theta n, window group g); grid covers N * G warps.
-template <bool TRACE>
-__global__ void __launch_bounds__(128) rollout_kernel(const DevModel* __restrict__ model, WinView win,
+// One warp per (theta n, window group g); grid covers N * G warps. MINB is the occupancy
+// target handed to the register allocator (CTAs of 128 threads per SM): 3 keeps every value in
+// registers (168), 4 caps at 128 registers with a few spills; the engine picks one at run time.
+template <bool TRACE, int MINB>
+__global__ void __launch_bounds__(128, MINB) rollout_kernel(const DevModel* __restrict__ model, WinView win,
                                                       const float* __restrict__ theta, int N, int G,
                                                       float* __restrict__ partial, float* __restrict__ trace,
                                                       unsigned long long* __restrict__ n_bad) {

@@ -36,10 +36,14 @@ ENGINE_API = {
     "spi_set_theta": (c_int, [c_void_p, c_void_p, c_int]),
     "spi_set_cost": (c_int, [c_void_p, c_int, POINTER(c_float)]),
     "spi_run": (c_int, [c_void_p]),
+    "spi_set_kernel_config": (c_int, [c_void_p, c_int]),
     "spi_run_trace": (c_int, [c_void_p, c_void_p]),
     "spi_read_costs": (c_int, [c_void_p, c_void_p, c_void_p]),
     "spi_sync": (c_int, [c_void_p, POINTER(c_int64)]),
     "spi_read_theta": (c_int, [c_void_p, c_void_p]),
+    "spi_sensitivity": (c_int, [c_void_p, c_void_p, c_int, POINTER(ctypes.c_int32), c_int, c_void_p, c_void_p]),
+    "spi_fisher": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_double, c_void_p, c_void_p, c_void_p,
+                           c_void_p]),
     "spi_probe_fp32_peak": (c_int, [POINTER(c_double)]),
     "spi_eval_windows_noalloc": (c_int, [POINTER(SpiRobot), c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int,
                                          c_float, c_void_p, c_int, c_int, POINTER(c_float), c_void_p, c_void_p,

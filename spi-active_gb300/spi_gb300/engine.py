@@ -72,6 +72,7 @@ class Engine:
                                                  wptr, W, H, float(norm) if norm else 0.0))
         self._keep = [init, target, actions, weight]   # alive until the copy kernels ran
         self.W, self.H = W, H
+        self.target = target
 
     def set_theta(self, theta):
         theta = _f32(theta, (int(theta.shape[0]), THETA_DIM), "theta", self.device)

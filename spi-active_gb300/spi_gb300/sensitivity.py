@@ -1,0 +1,118 @@
+"""State sensitivities, Fisher information and excitation scoring (spi_sensitivity / spi_fisher).
+
+The reference scores candidate excitations with a finite-difference Fisher proxy:
+main and auxiliary envs with theta + 0.1 (spigym/envs/sysid/active_sysid_openloop.py:29-80,
+402-426) and trace(J^T J) as the objective. Here J_w = d s_H / d theta comes from forward-mode
+derivatives of the rollout on the GPU, and a candidate is scored by log det of
+F = sum_w J_w^T Q J_w (D-optimal; trace is reported as well).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .data import standing_state
+from .robot import STATE_DIM, THETA_DIM
+
+
+def sensitivities(engine, theta, param_ids):
+    """J [N, W, 37, K] and final states xH [N, W, 37] for the engine's loaded windows."""
+    theta = torch.as_tensor(theta, dtype=torch.float32, device=engine.device).contiguous()
+    ids = (ctypes.c_int32 * len(param_ids))(*[int(i) for i in param_ids])
+    N, K = theta.shape[0], len(param_ids)
+    J = torch.empty((N, engine.W, STATE_DIM, K), device=engine.device)
+    xH = torch.empty((N, engine.W, STATE_DIM), device=engine.device)
+    _lib.check(engine.lib.spi_sensitivity(engine._h, theta.data_ptr(), N, ids, K, J.data_ptr(), xH.data_ptr()))
+    return J, xH
+
+
+def fisher(J, state_weight=None, eps=1e-9, stream=None):
+    """F [N, K, K] (FP32 accumulation), log det(F + eps I) and trace(F) (FP64) from J [N, W, 37, K]."""
+    J = J.contiguous()
+    N, W, S, K = J.shape
+    F = torch.empty((N, K, K), device=J.device)
+    logdet = torch.empty((N,), device=J.device, dtype=torch.float64)
+    trace = torch.empty((N,), device=J.device, dtype=torch.float64)
+    q = None
+    if state_weight is not None:
+        q = torch.as_tensor(state_weight, dtype=torch.float32, device=J.device).contiguous()
+    s = stream or torch.cuda.current_stream(J.device)
+    _lib.check(_lib.engine_lib().spi_fisher(J.data_ptr(), N, W, K, q.data_ptr() if q is not None else None,
+                                            float(eps), F.data_ptr(), logdet.data_ptr(), trace.data_ptr(),
+                                            ctypes.c_void_p(s.cuda_stream)))
+    return F, logdet, trace
+
+
+def block_weights(sq_weights):
+    """Per-state-component weights [37] from the six block weights (pos, quat, linvel, angvel, q, qd)."""
+    sizes = (3, 4, 3, 3, 12, 12)
+    return np.concatenate([np.full(n, w, np.float32) for n, w in zip(sizes, sq_weights)])
+
+
+class WindowCost(torch.autograd.Function):
+    """Weighted squared final-state error per theta sample, differentiable in theta.
+
+    forward(theta [N,13], engine, sq_weights) -> cost [N] = mean_w sum_i q_i (s_H,i - target_i)^2
+    over the engine's windows; the gradient comes from the forward-mode sensitivities.
+    """
+
+    @staticmethod
+    def forward(ctx, theta, engine, sq_weights):
+        J, xH = sensitivities(engine, theta.detach(), list(range(THETA_DIM)))
+        q = torch.as_tensor(block_weights(sq_weights), device=theta.device)
+        diff = xH - engine.target[None]
+        cost = (q * diff * diff).sum(-1).mean(1)
+        grad = 2.0 * torch.einsum("nwi,i,nwik->nk", diff, q, J) / engine.W
+        ctx.save_for_backward(grad)
+        return cost
+
+    @staticmethod
+    def backward(ctx, g):
+        (grad,) = ctx.saved_tensors
+        return g[:, None] * grad, None, None
+
+
+def multisine_actions(n_cand, T, control_dt, action_scale, n_comp=3, amp=(0.05, 0.4), freq=(0.5, 4.0), seed=0,
+                      settle=0):
+    """Candidate excitations: per joint a sum of n_comp sines (amplitudes in rad of joint target)."""
+    rng = np.random.default_rng(seed)
+    A = rng.uniform(amp[0], amp[1], (n_cand, 12, n_comp))
+    f = rng.uniform(freq[0], freq[1], (n_cand, 12, n_comp))
+    ph = rng.uniform(0.0, 2.0 * np.pi, (n_cand, 12, n_comp))
+    t = np.arange(T) * control_dt
+    s = np.sin(2.0 * np.pi * f[:, None] * t[None, :, None, None] + ph[:, None])      # [n, T, 12, c]
+    a = (A[:, None] * s).sum(-1) / action_scale
+    if settle:
+        a = np.concatenate([np.zeros((n_cand, settle, 12)), a], 1)
+    return a.astype(np.float32), dict(amp=A, freq=f, phase=ph)
+
+
+def score_excitations(engine, theta, actions, windows_per_cand=8, horizon=20, settle=100, param_ids=None,
+                      sq_weights=(10.0, 5.0, 0.1, 0.1, 1.0, 0.01), eps=1e-9):
+    """Fisher scores of candidate excitations at theta.
+
+    actions [n_cand, settle + windows_per_cand * horizon, 12]. Each candidate is rolled from a
+    standing start; windows of `horizon` steps start every `horizon` steps after `settle`.
+    Returns dict(logdet [n], trace [n], best, F [n,K,K]).
+    """
+    param_ids = list(range(THETA_DIM)) if param_ids is None else list(param_ids)
+    actions = np.asarray(actions, np.float32)
+    n, T = actions.shape[:2]
+    theta = np.asarray(theta, np.float32).reshape(1, THETA_DIM)
+    x0 = standing_state(n)
+    engine.load_windows(torch.from_numpy(x0), torch.from_numpy(actions), torch.from_numpy(x0))
+    _, _, tr = engine.evaluate(torch.from_numpy(theta), trace=True)          # [1, n, T, 37]
+    tr = tr[0]
+    starts = settle - 1 + horizon * np.arange(windows_per_cand)               # state index before each window
+    idx = torch.as_tensor(starts, device=tr.device)
+    init = tr[:, idx].reshape(-1, STATE_DIM)                                  # [n * wpc, 37]
+    act = torch.from_numpy(np.stack([actions[:, s + 1:s + 1 + horizon] for s in starts], 1)).reshape(-1, horizon, 12)
+    engine.load_windows(init, act, init)
+    J, _ = sensitivities(engine, torch.from_numpy(theta), param_ids)          # [1, n*wpc, 37, K]
+    J = J.reshape(n, windows_per_cand, STATE_DIM, len(param_ids))
+    F, logdet, trace = fisher(J, block_weights(sq_weights), eps)
+    ld = logdet.cpu().numpy()
+    return {"logdet": ld, "trace": trace.cpu().numpy(), "best": int(np.argmax(ld)), "F": F, "J": J}

@@ -1,0 +1,162 @@
+"""Multi-job identification workloads: uneven job mixes, served (batched) vs plain (one job at a time).
+
+* ``c2_specs`` draws jobs the way the uneven-batch workload describes them: population
+  U{256..4096}, windows U{16..512}, horizon U{5..50}, parameter dimension U{1..13} on the full
+  13-parameter model and priors, FP32, 30 CEM iterations each.
+* ``run_served`` admits jobs into the continuous-batching server as they arrive (all at t=0
+  for the batch workload, Poisson arrivals for the stream) and ticks until every job is done.
+* ``run_plain`` runs the same jobs one after another through the single-job engine (one
+  job per launch sequence, CUDA-graph iterations), in arrival order.
+Both report aggregate rollout-steps/s and per-job latency (completion - arrival).
+"""
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from .cem import CEM
+from .data import synthetic_windows
+from .engine import Engine
+from .robot import THETA_NOMINAL, THETA_PRIOR_HI, THETA_PRIOR_LO, SimConfig
+from .server import Server, cem_config
+
+
+@dataclass
+class JobSpec:
+    job_id: int
+    n_samples: int
+    n_windows: int
+    horizon: int
+    param_ids: list
+    iterations: int
+    seed: int
+    theta_true: np.ndarray
+    arrival: float = 0.0
+
+    @property
+    def rollout_steps(self) -> int:
+        return self.n_samples * self.n_windows * self.horizon * self.iterations
+
+
+def c2_specs(n_jobs, seed=0, iterations=30, pop=(256, 4096), windows=(16, 512), horizon=(5, 50), dims=(1, 13)):
+    rng = np.random.default_rng(seed)
+    specs = []
+    for j in range(n_jobs):
+        P = int(rng.integers(dims[0], dims[1] + 1))
+        ids = sorted(rng.choice(13, P, replace=False).tolist())
+        true = THETA_NOMINAL.copy()
+        true[ids] = THETA_PRIOR_LO[ids] + (THETA_PRIOR_HI[ids] - THETA_PRIOR_LO[ids]) * rng.random(P)
+        specs.append(JobSpec(j, int(rng.integers(pop[0], pop[1] + 1)), int(rng.integers(windows[0], windows[1] + 1)),
+                             int(rng.integers(horizon[0], horizon[1] + 1)), ids, iterations, 1000 + j, true))
+    return specs
+
+
+def poisson_arrivals(specs, rate, seed=0):
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, len(specs)))
+    for s, a in zip(specs, t):
+        s.arrival = float(a)
+    return specs
+
+
+class WindowBank:
+    """Ground-truth windows per job, generated on the GPU (each job its own theta and seed)."""
+
+    def __init__(self, cfg: SimConfig | None = None, device=None):
+        self.engine = Engine(cfg, device=device)
+        self.cache = {}
+
+    def get(self, spec: JobSpec):
+        key = spec.job_id
+        if key not in self.cache:
+            init, act, tgt = synthetic_windows(self.engine, spec.theta_true, spec.n_windows, spec.horizon,
+                                               n_traj=4, seed=spec.seed)
+            dev = self.engine.device
+            self.cache[key] = tuple(torch.from_numpy(a).to(dev) for a in (init, act, tgt))
+        return self.cache[key]
+
+
+def _cem_cfg(spec: JobSpec):
+    ids = spec.param_ids
+    return cem_config(spec.n_samples, ids, THETA_PRIOR_LO[ids], THETA_PRIOR_HI[ids], THETA_NOMINAL,
+                      seed=spec.seed, job_id=spec.job_id)
+
+
+def _summary(specs, latencies, wall, results=None):
+    steps = sum(s.rollout_steps for s in specs)
+    lat = np.array([latencies[s.job_id] for s in specs])
+    out = {"jobs": len(specs), "rollout_steps": int(steps), "wall_s": wall, "rollout_steps_per_s": steps / wall,
+           "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
+           "latency_mean_s": float(lat.mean())}
+    if results is not None:
+        out["results"] = results
+    return out
+
+
+def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=64, hbm_budget=150 << 30,
+               ctas_per_sm=0, items_per_claim=1, realtime=True):
+    """Continuous batching: admit on arrival (and free budget), one CEM iteration per tick for all."""
+    max_samples = max(s.n_samples for s in specs)
+    server = Server(cfg, max_slots=max_slots, max_samples=max_samples, hbm_budget_bytes=hbm_budget,
+                    device=bank.engine.device)
+    server.config(ctas_per_sm, items_per_claim)
+    jobs = {}
+    for s in specs:                       # windows ready before the clock starts
+        init, act, tgt = bank.get(s)
+        jobs[s.job_id] = (Server.make_job(init, act, tgt, _cem_cfg(s), s.iterations), (init, act, tgt))
+    pending = sorted(specs, key=lambda s: s.arrival)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    done, lat, results = 0, {}, {}
+    qi = 0
+    while done < len(specs):
+        now = time.perf_counter() - t0
+        while qi < len(pending) and (pending[qi].arrival <= now or not realtime):
+            spec = pending[qi]
+            if server.submit(jobs[spec.job_id][0]) is None:
+                break                     # no slot / budget: wait for a retirement
+            qi += 1
+        active, _ = server.stats()
+        server.tick()
+        if not active:
+            server.wait()
+            if qi < len(pending) and realtime:
+                time.sleep(max(0.0, min(pending[qi].arrival - (time.perf_counter() - t0), 0.002)))
+        for r in server.poll():
+            spec = specs[r["job_id"]] if specs[r["job_id"]].job_id == r["job_id"] else \
+                next(s for s in specs if s.job_id == r["job_id"])
+            lat[r["job_id"]] = time.perf_counter() - t0 - spec.arrival
+            results[r["job_id"]] = r
+            done += 1
+    wall = time.perf_counter() - t0
+    server.close()
+    return _summary(specs, lat, wall, results)
+
+
+def run_plain(specs, bank: WindowBank, cfg: SimConfig | None = None, graph=True):
+    """One job at a time through the single-job engine, in arrival order (FIFO)."""
+    eng = Engine(cfg, device=bank.engine.device)
+    order = sorted(specs, key=lambda s: s.arrival)
+    for s in order:
+        bank.get(s)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lat, results = {}, {}
+    for s in order:
+        now = time.perf_counter() - t0
+        if s.arrival > now:
+            time.sleep(s.arrival - now)
+        init, act, tgt = bank.get(s)
+        eng.load_windows(init, act, tgt)
+        ids = s.param_ids
+        cem = CEM(eng, s.n_samples, ids, THETA_PRIOR_LO[ids], THETA_PRIOR_HI[ids], THETA_NOMINAL, seed=s.seed,
+                  job_id=s.job_id)
+        cem.run(s.iterations, graph=graph)
+        r = cem.read()
+        lat[s.job_id] = time.perf_counter() - t0 - s.arrival
+        results[s.job_id] = r
+    wall = time.perf_counter() - t0
+    return _summary(specs, lat, wall, results)
