@@ -45,6 +45,14 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", choices=("c1", "c2", "c4"), default="c1")
+    ap.add_argument("--no-serving", action="store_true", help="c1: skip the served-vs-plain job mix")
+    ap.add_argument("--mix-jobs", type=int, default=16, help="c1: jobs in the served-vs-plain mix")
+    ap.add_argument("--mix-iters", type=int, default=10, help="c1: CEM iterations per job in the mix")
+    ap.add_argument("--c2-jobs", type=int, default=64)
+    ap.add_argument("--c4-rate", type=float, default=200.0, help="c4: arrivals per second")
+    ap.add_argument("--c4-jobs", type=int, default=64, help="c4: jobs in the stream")
+    ap.add_argument("--iters", type=int, default=30, help="c2/c4: CEM iterations per job")
     return ap.parse_args()
 
 
@@ -155,6 +163,52 @@ def _dist():
     torch.cuda.set_device(local)
     dist.init_process_group("nccl")
     return dist, dist.get_rank(), ws, local
+
+
+def served_vs_plain(specs, realtime, cfg=None):
+    """Run the same jobs served (continuous batching) and plain (one job at a time)."""
+    from spi_gb300.workloads import WindowBank, run_plain, run_served
+    bank = WindowBank(cfg)
+    served = run_served(specs, bank, cfg, realtime=realtime)
+    plain = run_plain(specs, bank, cfg)
+    errs = []
+    for s in specs:
+        a, b = served["results"][s.job_id]["best_cost"], plain["results"][s.job_id]["best_cost"]
+        errs.append(abs(a - b) / max(abs(b), 1e-30))
+    out = {}
+    for name, r in (("served", served), ("plain", plain)):
+        out[name] = {k: v for k, v in r.items() if k != "results"}
+    out["speedup_rollout_steps"] = served["rollout_steps_per_s"] / plain["rollout_steps_per_s"]
+    out["max_rel_cost_err_served_vs_plain"] = float(max(errs))
+    out["jobs"] = len(specs)
+    return out
+
+
+def run_multijob(args):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from spi_gb300.workloads import c2_specs, poisson_arrivals
+    torch.cuda.set_device(0)
+    if args.workload == "c2":
+        specs = c2_specs(args.c2_jobs, seed=2, iterations=args.iters)
+        desc = (f"c2: {args.c2_jobs} uneven jobs (pop U{{256..4096}}, W U{{16..512}}, H U{{5..50}}, "
+                f"P U{{1..13}}), {args.iters} CEM iterations each, all submitted at t=0")
+        realtime = False
+    else:
+        specs = poisson_arrivals(c2_specs(args.c4_jobs, seed=4, iterations=args.iters), args.c4_rate, seed=4)
+        desc = (f"c4: Poisson stream at {args.c4_rate:g} jobs/s, {args.c4_jobs} jobs from the c2 size "
+                f"distribution, {args.iters} CEM iterations each, 150 GB HBM admission budget")
+        realtime = True
+    with ClockSampler(0) as clocks:
+        r = served_vs_plain(specs, realtime)
+    served = r["served"]
+    line = {"metric": METRIC, "value": served["rollout_steps_per_s"], "unit": METRIC, "n_gpus": 1,
+            "steps": len(specs), "warmup": 0, "ms_per_step": served["wall_s"] * 1e3 / len(specs),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": desc, "step": "one identification job"},
+            "served_vs_plain": r, "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
 
 
 def run_reference(args):
@@ -288,6 +342,15 @@ def run_ours(args):
             "roofline": roof, "e2e": e2e, "gpu_launches": cem.launches_per_step * args.steps,
             "wall_s": wall, "nonfinite_rollouts": n_bad, "clocks": clocks.summary(),
             "cem": {"best_cost": cem.best_cost(), "theta_err": cem.theta_error(theta_true)}}
+    if ws == 1 and not args.no_serving:
+        from spi_gb300.workloads import c2_specs, small_specs
+        mix = served_vs_plain(c2_specs(args.mix_jobs, seed=2, iterations=args.mix_iters), False)
+        mix["workload"] = (f"{args.mix_jobs} jobs of the c2 size distribution, {args.mix_iters} CEM iterations "
+                           "each, all submitted at t=0")
+        small = served_vs_plain(small_specs(4 * args.mix_jobs, seed=3, iterations=args.mix_iters), False)
+        small["workload"] = (f"{4 * args.mix_jobs} small jobs (pop U{{64..512}}, W U{{8..64}}, H U{{5..20}}), "
+                             f"{args.mix_iters} CEM iterations each, all submitted at t=0")
+        line["served_vs_plain"] = {"c2_mix": mix, "small_jobs": small}
     if ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds, H)
     print(json.dumps(line), flush=True)
@@ -299,6 +362,8 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload in ("c2", "c4"):
+        run_multijob(args)
     else:
         run_ours(args)
 

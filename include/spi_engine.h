@@ -122,6 +122,13 @@ int spi_run(spi_engine* e);
 /* Same, also writing every control step's state to trace, device [N][W][H][37]. */
 int spi_run_trace(spi_engine* e, float* trace);
 
+/* Advance caller-owned states in place: state device [B][37] (world frame, the reference's
+ * root-state row + dof positions + dof velocities), actions device [B][steps][12], theta device
+ * [B][13]. The simulator step of the reference (spigym/simulator/base_simulator/
+ * base_simulator.py:121-150 under spigym/envs/legged_base_task/legged_robot_base.py:169-209).
+ * Asynchronous on the engine stream. */
+int spi_step_states(spi_engine* e, float* state, const float* actions, const float* theta, int B, int steps);
+
 /* Copy results of the last run (async on the engine stream): comp device [N][9] mean
  * components (may be NULL), cost device [N] scalar cost (may be NULL). */
 int spi_read_costs(spi_engine* e, float* comp, float* cost);
@@ -231,6 +238,10 @@ int spi_server_poll(spi_server* s, spi_job_result* results, int max, int32_t* n_
 int spi_server_wait(spi_server* s);
 /* Active job count and free budget. */
 int spi_server_stats(spi_server* s, int32_t* active, size_t* bytes_free);
+/* Admission cap on rollout work per tick, in (theta, 8-window group) items summed over active
+ * jobs (0 = no cap). A job that would exceed it waits (SPI_EBUDGET) unless nothing is active:
+ * once the GPU is full, admitting more jobs only slows every job down. */
+int spi_server_set_work_cap(spi_server* s, long long max_items);
 /* Persistent-grid shape: CTAs per SM (0 = occupancy maximum) and work items claimed per atomic. */
 int spi_server_config(spi_server* s, int ctas_per_sm, int items_per_claim);
 

@@ -32,6 +32,7 @@ SPI_INL Df& operator+=(Df& a, Df b) { a = a + b; return a; }
 SPI_INL Df& operator-=(Df& a, Df b) { a = a - b; return a; }
 SPI_INL bool operator>(Df a, Df b) { return a.v > b.v; }
 SPI_INL bool operator<=(Df a, Df b) { return a.v <= b.v; }
+SPI_INL bool operator<(Df a, Df b) { return a.v < b.v; }
 
 SPI_INL Df m_sqrt(Df x) {
   const float r = m_sqrt(x.v);

@@ -74,6 +74,14 @@ SPI_INL double m_fmax(double a, double b) { return fmax(a, b); }
 SPI_INL float m_fmin(float a, float b) { return fminf(a, b); }
 SPI_INL double m_fmin(double a, double b) { return fmin(a, b); }
 template <class T> SPI_INL T m_sel(bool c, T a, T b) { return c ? a : b; }
+// True if the predicate holds on any lane of the warp (the host emulation runs one lane).
+SPI_INL bool warp_any(bool p) {
+#if defined(__CUDA_ARCH__)
+  return __any_sync(0xffffffffu, p);
+#else
+  return p;
+#endif
+}
 template <class T> SPI_INL T m_clamp(T x, T lo, T hi) { return m_fmin(m_fmax(x, lo), hi); }
 
 // ---------------------------------------------------------------------------
@@ -197,12 +205,41 @@ template <class T> SPI_INL void add_to(Art<T>& a, const Art<T>& b) {
     for (int j = 0; j < 3; ++j) a.B.m[i][j] += b.B.m[i][j];
 }
 // X^T I X for the joint transform X = plucker(R^T, r): rotate by the active joint rotation,
-// then shift by the joint origin r (child origin in parent coordinates).
-template <int AX, class T> SPI_INL Art<T> art_to_parent(const Art<T>& I, T c, T s, V3<T> r) {
+// then shift by the joint origin r (child origin in parent coordinates):
+//   A' = A1 + P + P^T - [r]C1[r],  B' = B1 + [r]C1,  C' = C1,  P = [r] B1^T.
+template <int AX, int RM = 7, class T> SPI_INL Art<T> art_to_parent(const Art<T>& I, T c, T s, V3<T> r) {
   Art<T> o;
   S3<T> A1 = rot_sym<AX>(c, s, I.A);
   M3<T> B1 = rot_gen<AX>(c, s, I.B);
   S3<T> C1 = rot_sym<AX>(c, s, I.C);
+  if (RM == 4) {   // r = (0, 0, z)
+    const T z = r.z, zz = r.z * r.z;
+    o.A.xx = A1.xx - T(2) * z * B1.m[0][1] + zz * C1.yy;
+    o.A.yy = A1.yy + T(2) * z * B1.m[1][0] + zz * C1.xx;
+    o.A.zz = A1.zz;
+    o.A.xy = A1.xy + z * (B1.m[0][0] - B1.m[1][1]) - zz * C1.xy;
+    o.A.xz = A1.xz - z * B1.m[2][1];
+    o.A.yz = A1.yz + z * B1.m[2][0];
+    o.B.m[0][0] = B1.m[0][0] - z * C1.xy; o.B.m[0][1] = B1.m[0][1] - z * C1.yy; o.B.m[0][2] = B1.m[0][2] - z * C1.yz;
+    o.B.m[1][0] = B1.m[1][0] + z * C1.xx; o.B.m[1][1] = B1.m[1][1] + z * C1.xy; o.B.m[1][2] = B1.m[1][2] + z * C1.xz;
+    o.B.m[2][0] = B1.m[2][0]; o.B.m[2][1] = B1.m[2][1]; o.B.m[2][2] = B1.m[2][2];
+    o.C = C1;
+    return o;
+  }
+  if (RM == 2) {   // r = (0, y, 0)
+    const T y = r.y, yy = r.y * r.y;
+    o.A.xx = A1.xx + T(2) * y * B1.m[0][2] + yy * C1.zz;
+    o.A.yy = A1.yy;
+    o.A.zz = A1.zz - T(2) * y * B1.m[2][0] + yy * C1.xx;
+    o.A.xy = A1.xy + y * B1.m[1][2];
+    o.A.xz = A1.xz + y * (B1.m[2][2] - B1.m[0][0]) - yy * C1.xz;
+    o.A.yz = A1.yz - y * B1.m[1][0];
+    o.B.m[0][0] = B1.m[0][0] + y * C1.xz; o.B.m[0][1] = B1.m[0][1] + y * C1.yz; o.B.m[0][2] = B1.m[0][2] + y * C1.zz;
+    o.B.m[1][0] = B1.m[1][0]; o.B.m[1][1] = B1.m[1][1]; o.B.m[1][2] = B1.m[1][2];
+    o.B.m[2][0] = B1.m[2][0] - y * C1.xx; o.B.m[2][1] = B1.m[2][1] - y * C1.xy; o.B.m[2][2] = B1.m[2][2] - y * C1.xz;
+    o.C = C1;
+    return o;
+  }
   // P = skew(r) B1^T: column j = r x (row j of B1)
   V3<T> p0 = cross(r, row(B1, 0)), p1 = cross(r, row(B1, 1)), p2 = cross(r, row(B1, 2));
   // Q = skew(r) C1: column j = r x (column j of C1);  skew(r) C1 skew(r): column j = r x (C1 (r x e_j))
@@ -223,18 +260,37 @@ template <int AX, class T> SPI_INL Art<T> art_to_parent(const Art<T>& I, T c, T 
   o.C = C1;
   return o;
 }
+// Joint-origin sparsity. RM = 2: origin on the y axis (thigh joints), RM = 4: on the z axis
+// (calf joints), RM = 7: general (hip joints). The model builder checks the pattern.
+// r x u for an origin r with zero components skipped.
+template <int RM, class T> SPI_INL V3<T> rcross(V3<T> r, V3<T> u) {
+  if (RM == 2) return v3(r.y * u.z, T(0), -(r.y * u.x));
+  if (RM == 4) return v3(-(r.z * u.y), r.z * u.x, T(0));
+  return cross(r, u);
+}
+// u - r x w, with the known-zero component of r x w not subtracted.
+template <int RM, class T> SPI_INL V3<T> sub_rcross(V3<T> u, V3<T> r, V3<T> w) {
+  if (RM == 2) return v3(u.x - r.y * w.z, u.y, u.z + r.y * w.x);
+  if (RM == 4) return v3(u.x + r.z * w.y, u.y - r.z * w.x, u.z);
+  return u - cross(r, w);
+}
+template <int RM, class T> SPI_INL V3<T> add_rcross(V3<T> u, V3<T> r, V3<T> w) {
+  if (RM == 2) return v3(u.x + r.y * w.z, u.y, u.z - r.y * w.x);
+  if (RM == 4) return v3(u.x - r.z * w.y, u.y + r.z * w.x, u.z);
+  return u + cross(r, w);
+}
 // X^T f: child force to parent coordinates.
-template <int AX, class T> SPI_INL SV<T> force_to_parent(const SV<T>& f, T c, T s, V3<T> r) {
+template <int AX, int RM = 7, class T> SPI_INL SV<T> force_to_parent(const SV<T>& f, T c, T s, V3<T> r) {
   SV<T> o;
   o.v = rot<AX>(c, s, f.v);
-  o.w = rot<AX>(c, s, f.w) + cross(r, o.v);
+  o.w = add_rcross<RM>(rot<AX>(c, s, f.w), r, o.v);
   return o;
 }
 // X m: parent motion to child coordinates.
-template <int AX, class T> SPI_INL SV<T> motion_to_child(const SV<T>& m, T c, T s, V3<T> r) {
+template <int AX, int RM = 7, class T> SPI_INL SV<T> motion_to_child(const SV<T>& m, T c, T s, V3<T> r) {
   SV<T> o;
   o.w = rotT<AX>(c, s, m.w);
-  o.v = rotT<AX>(c, s, m.v - cross(r, m.w));
+  o.v = rotT<AX>(c, s, sub_rcross<RM>(m.v, r, m.w));
   return o;
 }
 
@@ -255,6 +311,7 @@ struct DevModel {
   float base_com[3], base_Ic[6];
   float base_m0, fixed_m, fixed_h[3], fixed_I[6];
   float foot_r, k, c, ct, mu, ramp_inv, imp_c;
+  float corner_reach;   // largest distance of a base-box corner from the base origin
   float kd_scale, act_scale, act_clip, hip_scale, fric_vel;
   float dt, g;
   int decimation, torque_speed, base_contact, inertia_follows_mass;
@@ -378,7 +435,7 @@ template <int AX, class T> SPI_INL SV<T> vel_product(const SV<T>& v, T qd) {
 }
 
 // One ABA backward step of joint k (axis AX): project out the joint, move to the parent.
-template <int AX, class T> SPI_INL void aba_back(Art<T>& IA, SV<T>& pA, const SV<T>& cb, T tau, T arm,
+template <int AX, int RM, class T> SPI_INL void aba_back(Art<T>& IA, SV<T>& pA, const SV<T>& cb, T tau, T arm,
                                                  T c, T s, V3<T> r, LegWork<T>& W, int k,
                                                  Art<T>* Iout, SV<T>* pout) {
   SV<T> U;
@@ -403,8 +460,8 @@ template <int AX, class T> SPI_INL void aba_back(Art<T>& IA, SV<T>& pA, const SV
   pa.w = pA.w + pa.w + uD * U.w;
   pa.v = pA.v + pa.v + uD * U.v;
   W.U[k] = U; W.invD[k] = invD; W.u[k] = u;
-  *Iout = art_to_parent<AX>(Ia, c, s, r);
-  *pout = force_to_parent<AX>(pa, c, s, r);
+  *Iout = art_to_parent<AX, RM>(Ia, c, s, r);
+  *pout = force_to_parent<AX, RM>(pa, c, s, r);
 }
 
 // ---------------------------------------------------------------------------
@@ -422,8 +479,8 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
   V3<T> r0 = leg_org<T>(M, 0, leg), r1 = leg_org<T>(M, 1, leg), r2 = leg_org<T>(M, 2, leg);
   // body velocities (body coordinates) and velocity-product accelerations
   SV<T> v0 = motion_to_child<0>(B.nu, W.c[0], W.s[0], r0); v0.w.x = v0.w.x + L.qd[0];
-  SV<T> v1 = motion_to_child<1>(v0, W.c[1], W.s[1], r1);   v1.w.y = v1.w.y + L.qd[1];
-  SV<T> v2 = motion_to_child<1>(v1, W.c[2], W.s[2], r2);   v2.w.y = v2.w.y + L.qd[2];
+  SV<T> v1 = motion_to_child<1, 2>(v0, W.c[1], W.s[1], r1);   v1.w.y = v1.w.y + L.qd[1];
+  SV<T> v2 = motion_to_child<1, 4>(v1, W.c[2], W.s[2], r2);   v2.w.y = v2.w.y + L.qd[2];
   W.cb[0] = vel_product<0>(v0, L.qd[0]);
   W.cb[1] = vel_product<1>(v1, L.qd[1]);
   W.cb[2] = vel_product<1>(v2, L.qd[2]);
@@ -452,16 +509,18 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
   pA.w = pA.w - cross(fc, Fc);
   pA.v = pA.v - Fc;
   Art<T> Ip; SV<T> pp;
-  aba_back<1>(IA, pA, W.cb[2], tau[2], P.arm, W.c[2], W.s[2], r2, W, 2, &Ip, &pp);
+  aba_back<1, 4>(IA, pA, W.cb[2], tau[2], P.arm, W.c[2], W.s[2], r2, W, 2, &Ip, &pp);
   IA = leg_rigid<T>(M, 1, leg); add_to(IA, Ip);
   pA = leg_bias(M, 1, leg, v1); pA.w = pA.w + pp.w; pA.v = pA.v + pp.v;
-  aba_back<1>(IA, pA, W.cb[1], tau[1], P.arm, W.c[1], W.s[1], r1, W, 1, &Ip, &pp);
+  aba_back<1, 2>(IA, pA, W.cb[1], tau[1], P.arm, W.c[1], W.s[1], r1, W, 1, &Ip, &pp);
   IA = leg_rigid<T>(M, 0, leg); add_to(IA, Ip);
   pA = leg_bias(M, 0, leg, v0); pA.w = pA.w + pp.w; pA.v = pA.v + pp.v;
   LegOut<T> out;
-  aba_back<0>(IA, pA, W.cb[0], tau[0], P.arm, W.c[0], W.s[0], r0, W, 0, &out.I, &out.p);
-  // two of the eight base-box corners
-  if (M.base_contact) {
+  aba_back<0, 7>(IA, pA, W.cb[0], tau[0], P.arm, W.c[0], W.s[0], r0, W, 0, &out.I, &out.p);
+  // two of the eight base-box corners; a corner can only reach the ground when the base origin
+  // is lower than the box's half-diagonal, so a warp whose rollouts are all higher skips them
+  // (a corner off the ground adds exactly zero force and zero implicit mass)
+  if (M.base_contact && warp_any(B.p.z < T(M.corner_reach))) {
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
       const float* cc = M.corner[2 * leg + j];
@@ -561,11 +620,11 @@ SPI_INL void phase_c(const DevModel& M, int leg, const SV<T>& a0, const LegWork<
   a.w = a.w + W.cb[0].w; a.v = a.v + W.cb[0].v;
   qdd[0] = (W.u[0] - dot(W.U[0].w, a.w) - dot(W.U[0].v, a.v)) * W.invD[0];
   a.w.x = a.w.x + qdd[0];
-  a = motion_to_child<1>(a, W.c[1], W.s[1], leg_org<T>(M, 1, leg));
+  a = motion_to_child<1, 2>(a, W.c[1], W.s[1], leg_org<T>(M, 1, leg));
   a.w = a.w + W.cb[1].w; a.v = a.v + W.cb[1].v;
   qdd[1] = (W.u[1] - dot(W.U[1].w, a.w) - dot(W.U[1].v, a.v)) * W.invD[1];
   a.w.y = a.w.y + qdd[1];
-  a = motion_to_child<1>(a, W.c[2], W.s[2], leg_org<T>(M, 2, leg));
+  a = motion_to_child<1, 4>(a, W.c[2], W.s[2], leg_org<T>(M, 2, leg));
   a.w = a.w + W.cb[2].w; a.v = a.v + W.cb[2].v;
   qdd[2] = (W.u[2] - dot(W.U[2].w, a.w) - dot(W.U[2].v, a.v)) * W.invD[2];
   T dt = T(M.dt);

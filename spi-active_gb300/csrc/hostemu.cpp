@@ -32,6 +32,7 @@ inline Cf& operator+=(Cf& a, Cf b) { a = a + b; return a; }
 inline Cf& operator-=(Cf& a, Cf b) { a = a - b; return a; }
 inline bool operator>(Cf a, Cf b) { return a.v > b.v; }
 inline bool operator<=(Cf a, Cf b) { return a.v <= b.v; }
+inline bool operator<(Cf a, Cf b) { return a.v < b.v; }
 inline Cf m_sqrt(Cf x) { ++Cf::n; return Cf(std::sqrt(x.v)); }
 inline Cf m_tanh(Cf x) { ++Cf::n; return Cf(std::tanh(x.v)); }
 inline void m_sincos(Cf x, Cf* s, Cf* c) { Cf::n += 2; *s = Cf(std::sin(x.v)); *c = Cf(std::cos(x.v)); }
@@ -144,6 +145,37 @@ int spi_hostemu_count_ops(const spi_robot* robot, const double* state, const dou
   Cf::n = 0;
   substep(M, B, L, bp, lp, act);
   if (per_substep) *per_substep = Cf::n;
+  return SPI_OK;
+}
+
+// Algorithmic FP operations of one substep per phase: [A (all four legs), B (base), C (all legs)].
+int spi_hostemu_count_phases(const spi_robot* robot, const double* state, const double* theta,
+                             const double* act12, long long* out3) {
+  DevModel M;
+  const char* why = "";
+  int rc = build_dev_model(*robot, &M, &why);
+  if (rc) return rc;
+  BaseState<Cf> B;
+  LegState<Cf> L[4];
+  BaseParams<Cf> bp;
+  LegParams<Cf> lp[4];
+  load_rollout(M, state, theta, B, L, bp, lp);
+  Cf act[12];
+  for (int j = 0; j < 12; ++j) act[j] = Cf(act12[j]);
+  LegWork<Cf> W[4];
+  LegOut<Cf> o[4];
+  Cf::n = 0;
+  for (int leg = 0; leg < 4; ++leg) o[leg] = phase_a(M, leg, B, L[leg], lp[leg], act + 3 * leg, W[leg]);
+  add_out(o[0], o[1]);
+  add_out(o[2], o[3]);
+  add_out(o[0], o[2]);
+  out3[0] = Cf::n;
+  Cf::n = 0;
+  SV<Cf> a0 = phase_b(M, bp, o[0], B);
+  out3[1] = Cf::n;
+  Cf::n = 0;
+  for (int leg = 0; leg < 4; ++leg) phase_c(M, leg, a0, W[leg], L[leg]);
+  out3[2] = Cf::n;
   return SPI_OK;
 }
 

@@ -2,6 +2,7 @@
 // engine and the host emulation.
 #pragma once
 
+#include <math.h>
 #include <string.h>
 
 #include "dynamics.cuh"
@@ -26,12 +27,26 @@ inline int build_dev_model(const spi_robot& r, DevModel* M, const char** why) {
       M->tlim[k][leg] = r.torque_limit[b];
       M->vlim[k][leg] = r.velocity_limit[b];
       if (!(r.body_mass[b] > 0.0f)) { *why = "leg body mass must be > 0"; return SPI_EINVAL; }
+      // the kernel's transforms assume thigh joints offset along y and calf joints along z
+      if (k == 1 && (r.body_origin[b][0] != 0.0f || r.body_origin[b][2] != 0.0f)) {
+        *why = "thigh joint origins must lie on the hip frame's y axis"; return SPI_EINVAL;
+      }
+      if (k == 2 && (r.body_origin[b][0] != 0.0f || r.body_origin[b][1] != 0.0f)) {
+        *why = "calf joint origins must lie on the thigh frame's z axis"; return SPI_EINVAL;
+      }
       if (r.torque_speed && !(r.velocity_limit[b] > 0.0f)) {
         *why = "velocity_limit must be > 0 with torque_speed"; return SPI_EINVAL;
       }
     }
   }
   memcpy(M->corner, r.corners, sizeof(M->corner));
+  M->corner_reach = 0.0f;
+  for (int i = 0; i < 8; ++i) {
+    const float d = sqrtf(r.corners[i][0] * r.corners[i][0] + r.corners[i][1] * r.corners[i][1] +
+                          r.corners[i][2] * r.corners[i][2]);
+    M->corner_reach = d > M->corner_reach ? d : M->corner_reach;
+  }
+  M->corner_reach *= 1.001f;   // margin over float rounding of the corner coordinates
   memcpy(M->foot, r.foot, sizeof(M->foot));
   memcpy(M->gain, r.motor_gain, sizeof(M->gain));
   memcpy(M->tanh_a, r.tanh_a, sizeof(M->tanh_a));

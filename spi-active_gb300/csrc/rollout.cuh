@@ -174,31 +174,48 @@ __global__ void __launch_bounds__(128, MINB) rollout_kernel(const DevModel* __re
                        partial + ((size_t)n * G + g) * SPI_N_COMP, tr, n_bad);
 }
 
-// comp[n][k] = sum_g partial[n][g][k] / norm; cost[n] from the cost mode.
-static __global__ void finalize_costs(const float* __restrict__ partial, int N, int G, float norm, int mode,
-                               float w0, float w1, float w2, float w3, float w4, float w5,
-                               float* __restrict__ comp, float* __restrict__ cost) {
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (n >= N) return;
+// comp[n][k] = sum_g partial[n][g][k] / norm; cost from the cost mode. Shared by every
+// finalize kernel, with the weighted sum written as explicit fmaf so that the single-job
+// engine and the server produce bitwise-identical costs.
+__device__ __forceinline__ void finalize_one(const float* __restrict__ partial, int n, int G, float norm, int mode,
+                                             const float* w, float* __restrict__ comp, float* __restrict__ cost) {
   float c[SPI_N_COMP];
 #pragma unroll
   for (int k = 0; k < SPI_N_COMP; ++k) c[k] = 0.f;
   for (int g = 0; g < G; ++g) {
     const float* p = partial + ((size_t)n * G + g) * SPI_N_COMP;
 #pragma unroll
-    for (int k = 0; k < SPI_N_COMP; ++k) c[k] += p[k];
+    for (int k = 0; k < SPI_N_COMP; ++k) c[k] = __fadd_rn(c[k], p[k]);
   }
-  const float inv = 1.0f / norm;
+  const float inv = __frcp_rn(norm);
 #pragma unroll
-  for (int k = 0; k < SPI_N_COMP; ++k) c[k] *= inv;
+  for (int k = 0; k < SPI_N_COMP; ++k) c[k] = __fmul_rn(c[k], inv);
   if (comp) {
 #pragma unroll
     for (int k = 0; k < SPI_N_COMP; ++k) comp[(size_t)n * SPI_N_COMP + k] = c[k];
   }
   if (cost) {
-    cost[n] = mode == 0 ? 10.f * c[0] + 5.f * c[1] + 1.f * c[2]
-                        : w0 * c[3] + w1 * c[4] + w2 * c[5] + w3 * c[6] + w4 * c[7] + w5 * c[8];
+    float v;
+    if (mode == 0) {
+      v = __fmul_rn(10.f, c[0]);
+      v = __fmaf_rn(5.f, c[1], v);
+      v = __fadd_rn(v, c[2]);
+    } else {
+      v = __fmul_rn(w[0], c[3]);
+#pragma unroll
+      for (int k = 1; k < 6; ++k) v = __fmaf_rn(w[k], c[3 + k], v);
+    }
+    cost[n] = v;
   }
+}
+
+static __global__ void finalize_costs(const float* __restrict__ partial, int N, int G, float norm, int mode,
+                                      float w0, float w1, float w2, float w3, float w4, float w5,
+                                      float* __restrict__ comp, float* __restrict__ cost) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= N) return;
+  const float w[6] = {w0, w1, w2, w3, w4, w5};
+  finalize_one(partial, n, G, norm, mode, w, comp, cost);
 }
 
 }  // namespace spi

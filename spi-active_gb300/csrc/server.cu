@@ -74,7 +74,7 @@ __global__ void srv_fill(float* p, float v, int n) {
 }
 
 // Persistent rollout over the work items of every active slot.
-__global__ void __launch_bounds__(128) server_rollout_kernel(const DevModel* __restrict__ model,
+__global__ void __launch_bounds__(128, 3) server_rollout_kernel(const DevModel* __restrict__ model,
                                                              const SlotDesc* __restrict__ slots,
                                                              const int* __restrict__ order,
                                                              const TickInfo* __restrict__ info,
@@ -113,21 +113,8 @@ __global__ void server_finalize_kernel(const SlotDesc* __restrict__ slots, int m
   const SlotDesc& S = slots[blockIdx.y];
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (!S.active || n >= S.N) return;
-  float c[SPI_N_COMP];
-#pragma unroll
-  for (int k = 0; k < SPI_N_COMP; ++k) c[k] = 0.f;
-  for (int g = 0; g < S.G; ++g) {
-#pragma unroll
-    for (int k = 0; k < SPI_N_COMP; ++k) c[k] += S.partial[((size_t)n * S.G + g) * SPI_N_COMP + k];
-  }
-  const float inv = 1.0f / S.norm;
-#pragma unroll
-  for (int k = 0; k < SPI_N_COMP; ++k) {
-    c[k] *= inv;
-    S.comp[(size_t)n * SPI_N_COMP + k] = c[k];
-  }
-  S.cost[n] = mode == 0 ? 10.f * c[0] + 5.f * c[1] + 1.f * c[2]
-                        : w0 * c[3] + w1 * c[4] + w2 * c[5] + w3 * c[6] + w4 * c[7] + w5 * c[8];
+  const float w[6] = {w0, w1, w2, w3, w4, w5};
+  finalize_one(S.partial, n, S.G, S.norm, mode, w, S.comp, S.cost);
 }
 
 inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -174,8 +161,10 @@ struct spi_server {
   CemState* h_cem_out = nullptr;   // pinned, per slot
   int* h_zero = nullptr;           // pinned 0 (clears CemState::active)
   cudaEvent_t staging_free = nullptr;
+  cudaEvent_t tick_done[2] = {nullptr, nullptr};   // at most two ticks in flight
   cudaGraphExec_t graph = nullptr;
   int grid = 0, ctas_per_sm = 0, items_per_claim = 1;
+  long long max_items = 0;         // admission cap on work items per tick (0: none)
   int cost_mode = 1;
   float sq_w[6] = {10.f, 5.f, 0.1f, 0.1f, 1.f, 0.01f};
   long long ticks = 0;
@@ -192,6 +181,7 @@ void free_server(spi_server* s) {
   }
   if (s->graph) cudaGraphExecDestroy(s->graph);
   if (s->staging_free) cudaEventDestroy(s->staging_free);
+  for (auto& ev : s->tick_done) if (ev) cudaEventDestroy(ev);
   if (s->capture) cudaStreamDestroy(s->capture);
   cudaFree(s->d_model); cudaFree(s->d_slots); cudaFree(s->d_order); cudaFree(s->d_info);
   cudaFree(s->d_counter); cudaFree(s->d_bad); cudaFree(s->d_cem);
@@ -294,6 +284,8 @@ int spi_server_create(const spi_robot* robot, int max_slots, int max_samples, si
   SRV_TRY(cudaMallocHost(&s->h_zero, sizeof(int)));
   SRV_TRY(cudaStreamCreateWithFlags(&s->capture, cudaStreamNonBlocking));
   SRV_TRY(cudaEventCreateWithFlags(&s->staging_free, cudaEventDisableTiming));
+  SRV_TRY(cudaEventCreateWithFlags(&s->tick_done[0], cudaEventDisableTiming));
+  SRV_TRY(cudaEventCreateWithFlags(&s->tick_done[1], cudaEventDisableTiming));
   SRV_TRY(cudaFuncSetAttribute(cem_refit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                CEM_MAX_SAMPLES * (int)sizeof(unsigned long long)));
   for (auto& sl : s->slots) SRV_TRY(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
@@ -325,6 +317,12 @@ int spi_server_set_cost(spi_server* s, int mode, const float* sq_weights) {
   return SPI_OK;
 }
 
+int spi_server_set_work_cap(spi_server* s, long long max_items) {
+  if (!s || max_items < 0) return set_error(SPI_EINVAL, "spi_server_set_work_cap: bad argument");
+  s->max_items = max_items;
+  return SPI_OK;
+}
+
 int spi_server_config(spi_server* s, int ctas_per_sm, int items_per_claim) {
   if (!s) return set_error(SPI_EINVAL, "null server");
   if (ctas_per_sm < 0 || items_per_claim < 1 || items_per_claim > 64)
@@ -352,6 +350,15 @@ int spi_server_submit(spi_server* s, const spi_job* job, int32_t* slot_out) {
   if (slot < 0 || s->used + L.total > s->budget)
     return set_error(SPI_EBUDGET, "spi_server_submit: %s (need %zu bytes, %zu free)",
                      slot < 0 ? "no free slot" : "over the HBM budget", L.total, s->budget - s->used);
+  if (s->max_items > 0) {
+    long long items = 0;
+    for (const auto& o : s->slots)
+      if (o.active) items += (long long)o.desc.N * o.desc.G;
+    const long long mine = (long long)c.n_samples * ((job->W + 7) / 8);
+    if (items > 0 && items + mine > s->max_items)
+      return set_error(SPI_EBUDGET, "spi_server_submit: GPU work cap reached (%lld + %lld items > %lld)", items,
+                       mine, s->max_items);
+  }
   CemState& h = s->h_cem_in[slot];
   memset(&h, 0, sizeof(h));
   unsigned seen = 0;
@@ -433,6 +440,10 @@ int spi_server_submit(spi_server* s, const spi_job* job, int32_t* slot_out) {
 
 int spi_server_tick(spi_server* s) {
   if (!s) return set_error(SPI_EINVAL, "null server");
+  // keep the host at most two ticks ahead of the device, so retirements (decided from host
+  // counts) and their result copies are observed within a tick of happening
+  cudaError_t we = cudaEventSynchronize(s->tick_done[s->ticks & 1]);
+  if (we != cudaSuccess) return cuda_error(we, "spi_server_tick: wait");
   // retire finished slots: copy the CEM state out, deactivate, free the slot memory
   for (int i = 0; i < s->max_slots; ++i) {
     SlotHost& sl = s->slots[i];
@@ -480,6 +491,7 @@ int spi_server_tick(spi_server* s) {
   int rc = build_graph(s);
   if (rc) return rc;
   ce = cudaGraphLaunch(s->graph, s->stream);
+  if (ce == cudaSuccess) ce = cudaEventRecord(s->tick_done[s->ticks & 1], s->stream);
   if (ce != cudaSuccess) return cuda_error(ce, "spi_server_tick: launch");
   for (int i : act) s->slots[i].remaining -= 1;
   ++s->ticks;

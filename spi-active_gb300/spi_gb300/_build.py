@@ -21,9 +21,10 @@ LIB_DIR = PKG / "_lib"
 ENGINE_SO = LIB_DIR / "libspi_engine.so"
 HOSTEMU_SO = LIB_DIR / "libspi_hostemu.so"
 
-CU_SOURCES = ("engine.cu", "cem.cu", "server.cu", "sensitivity.cu", "probe.cu", "noalloc.cu")
+CU_SOURCES = ("engine.cu", "cem.cu", "server.cu", "sensitivity.cu", "step.cu", "probe.cu", "noalloc.cu")
 ARCH = ("-gencode", "arch=compute_103a,code=sm_103a")
-NVCC_FLAGS = ARCH + ("-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+NVCC_FLAGS = ARCH + ("-O3", "-lineinfo", "-std=c++17", "-ftz=true", "-prec-div=false", "-prec-sqrt=false",
+                     "-Xcompiler", "-fPIC",
                      f"-I{INCLUDE}", f"-I{CSRC}")
 CXX_FLAGS = ("-O2", "-std=c++17", "-shared", "-fPIC", "-Wall", "-Wno-unknown-pragmas",
              f"-I{INCLUDE}", f"-I{CSRC}")

@@ -41,6 +41,7 @@ ENGINE_API = {
     "spi_read_costs": (c_int, [c_void_p, c_void_p, c_void_p]),
     "spi_sync": (c_int, [c_void_p, POINTER(c_int64)]),
     "spi_read_theta": (c_int, [c_void_p, c_void_p]),
+    "spi_step_states": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int]),
     "spi_sensitivity": (c_int, [c_void_p, c_void_p, c_int, POINTER(ctypes.c_int32), c_int, c_void_p, c_void_p]),
     "spi_fisher": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_double, c_void_p, c_void_p, c_void_p,
                            c_void_p]),

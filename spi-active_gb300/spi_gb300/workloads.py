@@ -54,6 +54,12 @@ def c2_specs(n_jobs, seed=0, iterations=30, pop=(256, 4096), windows=(16, 512), 
     return specs
 
 
+def small_specs(n_jobs, seed=0, iterations=30):
+    """Small jobs (population U{64..512}, windows U{8..64}, horizon U{5..20}): each alone leaves
+    most of the GPU idle, the regime continuous batching is for."""
+    return c2_specs(n_jobs, seed=seed, iterations=iterations, pop=(64, 512), windows=(8, 64), horizon=(5, 20))
+
+
 def poisson_arrivals(specs, rate, seed=0):
     rng = np.random.default_rng(seed)
     t = np.cumsum(rng.exponential(1.0 / rate, len(specs)))
@@ -96,13 +102,21 @@ def _summary(specs, latencies, wall, results=None):
     return out
 
 
+def default_work_cap(device=None):
+    """Work items (8-window warps) that keep every SM busy for ~8 waves of resident warps."""
+    props = torch.cuda.get_device_properties(device or torch.cuda.current_device())
+    return 8 * props.multi_processor_count * 12
+
+
 def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=64, hbm_budget=150 << 30,
-               ctas_per_sm=0, items_per_claim=1, realtime=True):
-    """Continuous batching: admit on arrival (and free budget), one CEM iteration per tick for all."""
+               ctas_per_sm=0, items_per_claim=1, realtime=True, work_cap=None):
+    """Continuous batching: admit on arrival while HBM budget, a slot and GPU work capacity are free;
+    one CEM iteration per tick for every admitted job."""
     max_samples = max(s.n_samples for s in specs)
     server = Server(cfg, max_slots=max_slots, max_samples=max_samples, hbm_budget_bytes=hbm_budget,
                     device=bank.engine.device)
     server.config(ctas_per_sm, items_per_claim)
+    server.set_work_cap(default_work_cap(bank.engine.device) if work_cap is None else work_cap)
     jobs = {}
     for s in specs:                       # windows ready before the clock starts
         init, act, tgt = bank.get(s)

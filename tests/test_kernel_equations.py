@@ -14,7 +14,7 @@ from oracle import spatial
 from oracle import sysid as osy
 from helpers import random_theta
 
-FLOPS_PER_SUBSTEP = 9109      # instrumented count of csrc/dynamics.cuh, default configuration
+FLOPS_PER_SUBSTEP = 7053      # instrumented count of csrc/dynamics.cuh, default configuration, standing state (base-box corners off the ground)
 
 
 def _emu(built, cfg, x0, acts, th):
