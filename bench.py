@@ -171,15 +171,20 @@ def served_vs_plain(specs, realtime, cfg=None):
     bank = WindowBank(cfg)
     served = run_served(specs, bank, cfg, realtime=realtime)
     plain = run_plain(specs, bank, cfg)
-    errs = []
+    ratios = []
     for s in specs:
         a, b = served["results"][s.job_id]["best_cost"], plain["results"][s.job_id]["best_cost"]
-        errs.append(abs(a - b) / max(abs(b), 1e-30))
+        ratios.append(a / max(b, 1e-30))
+    ratios = np.array(ratios)
     out = {}
     for name, r in (("served", served), ("plain", plain)):
         out[name] = {k: v for k, v in r.items() if k != "results"}
     out["speedup_rollout_steps"] = served["rollout_steps_per_s"] / plain["rollout_steps_per_s"]
-    out["max_rel_cost_err_served_vs_plain"] = float(max(errs))
+    # The served and plain kernels are separate compilations of the same rollout; ulp-level
+    # rounding differences change a CEM's elite set, after which the two searches part ways.
+    # The ratio of their final best costs therefore checks that both converge equally well.
+    out["best_cost_ratio_served_over_plain"] = {"median": float(np.median(ratios)), "min": float(ratios.min()),
+                                                "max": float(ratios.max())}
     out["jobs"] = len(specs)
     return out
 
@@ -196,9 +201,11 @@ def run_multijob(args):
                 f"P U{{1..13}}), {args.iters} CEM iterations each, all submitted at t=0")
         realtime = False
     else:
-        specs = poisson_arrivals(c2_specs(args.c4_jobs, seed=4, iterations=args.iters), args.c4_rate, seed=4)
+        specs = poisson_arrivals(c2_specs(args.c4_jobs, seed=4, iterations=args.iters), args.c4_rate, seed=4,
+                                 fisher_frac=0.2)
         desc = (f"c4: Poisson stream at {args.c4_rate:g} jobs/s, {args.c4_jobs} jobs from the c2 size "
-                f"distribution, {args.iters} CEM iterations each, 150 GB HBM admission budget")
+                f"distribution, {args.iters} CEM iterations each, 20% also score 32 candidate excitations "
+                f"(Fisher log det at the identified theta), 150 GB HBM admission budget")
         realtime = True
     with ClockSampler(0) as clocks:
         r = served_vs_plain(specs, realtime)
@@ -255,6 +262,11 @@ def run_ours(args):
               elite_frac=C1["elite_frac"], seed=4321 + rank)
     flush = torch.empty(256 * 1024 * 1024 // 4, device=dev)
     stream = torch.cuda.current_stream(dev)
+    # pick the rollout-kernel occupancy variant on this workload (outside the timed region)
+    from spi_gb300.autotune import tune_engine
+    cem.sample()
+    variant, variant_ms = tune_engine(eng, use_cache=False)
+    cem.sample()             # the tuning runs do not advance the CEM state
 
     for _ in range(args.warmup):
         cem.step()
@@ -324,7 +336,10 @@ def run_ours(args):
     peak = probe_fp32_peak()
     achieved = steps_per_iter * fl / (kmean * 1e-3)
     roof = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": None,
+            "frac": achieved / peak, "traffic": 422656,
+            "traffic_note": "dram read+write bytes per launch from ncu on 1024 theta x the same 256 windows "
+                            "(profiles/rollout_kernel_1024x256xH20_after_sparse.md); the window set is read once "
+                            "and theta / partials stay in L2, so traffic does not scale with theta",
             "kernel": "rollout_kernel (+finalize_costs)", "kernel_ms": kmean,
             "flops_per_rollout_step": fl,
             "peak_source": "measured FP32 FMA-loop probe on this GPU (no FP32 entry in MEASURED_PEAKS.json)"}
@@ -338,7 +353,8 @@ def run_ours(args):
             "config": {"workload": "c1", "n_theta": N, "n_windows": W, "horizon": H, "substeps": cfg.decimation,
                        "n_params": 13, "elite_frac": C1["elite_frac"],
                        "step": "one CEM iteration (rollouts + cost + refit + resample)",
-                       "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{ws}"},
+                       "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{ws}",
+                       "kernel_variant": {"ctas_per_sm_target": variant, "tuning_ms": variant_ms}},
             "roofline": roof, "e2e": e2e, "gpu_launches": cem.launches_per_step * args.steps,
             "wall_s": wall, "nonfinite_rollouts": n_bad, "clocks": clocks.summary(),
             "cem": {"best_cost": cem.best_cost(), "theta_err": cem.theta_error(theta_true)}}

@@ -185,6 +185,10 @@ int spi_sensitivity(spi_engine* e, const float* theta, int N, const int32_t* par
                     float* xH);
 int spi_fisher(const float* J, int N, int W, int K, const float* state_weight, double eps, float* F,
                double* logdet, double* trace, void* stream);
+/* As spi_fisher; tensor_cores = 1 accumulates J^T Q J on the tensor cores (BF16 operands, FP32
+ * accumulation, warp-level mma m16n8k16), 0 on the CUDA cores in FP32. */
+int spi_fisher_ex(const float* J, int N, int W, int K, const float* state_weight, double eps, int tensor_cores,
+                  float* F, double* logdet, double* trace, void* stream);
 
 /* ---- continuous-batching identification server ------------------------------------------
  * Many sysid jobs of uneven population, window count, horizon and parameter dimension share
@@ -244,6 +248,8 @@ int spi_server_stats(spi_server* s, int32_t* active, size_t* bytes_free);
 int spi_server_set_work_cap(spi_server* s, long long max_items);
 /* Persistent-grid shape: CTAs per SM (0 = occupancy maximum) and work items claimed per atomic. */
 int spi_server_config(spi_server* s, int ctas_per_sm, int items_per_claim);
+/* Rollout-kernel occupancy variant (3 or 4 CTAs of 128 threads per SM), as spi_set_kernel_config. */
+int spi_server_set_kernel_config(spi_server* s, int min_blocks);
 
 /* ---- evaluation without any device allocation ---------------------------------------
  * No counterpart in the reference. For callers that must not let a library call cudaMalloc:

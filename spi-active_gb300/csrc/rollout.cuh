@@ -1,6 +1,6 @@
 // rollout.cuh -- warp-level rollout of (theta, window) pairs and the fixed-order cost reduction.
 //
-// Lane layout: four lanes per rollout (lane & 3 = leg FL, FR, RL, RR), eight rollouts per
+// Lane layout (CTAs of 128 threads): four lanes per rollout (lane & 3 = leg FL, FR, RL, RR), eight rollouts per
 // warp (lane >> 2 = slot). A warp evaluates one theta sample against eight consecutive
 // windows ("window group"). Per physics substep each lane runs phase A for its leg, the
 // quad sums the four leg contributions with two xor-shuffles (bitwise identical on all four
@@ -64,6 +64,33 @@ __device__ __forceinline__ void load_model_smem(DevModel* dst, const DevModel* _
 // Roll one warp's eight windows for theta th13 (13 floats, same for the warp) and write the
 // window group's weighted error components to partial9 (lane 0). trace, when non-null, is
 // the [W][H][37] block of this theta.
+// One physics substep of a lane quad: phase A (leg), quad reduction, phase B (base solve),
+// phase C (leg). The 48-float LegWork of each lane is parked in shared memory between phase A
+// and phase C so that its registers are free during the reduction and the base solve;
+// [field][thread] layout keeps the accesses conflict-free. Blocks must be 128 threads. Every
+// kernel that steps the dynamics calls this one function.
+__device__ __forceinline__ void substep(const DevModel& M, int leg, BaseState<float>& B, LegState<float>& L,
+                                        const BaseParams<float>& bp, const LegParams<float>& lp,
+                                        const float act[3]) {
+  __shared__ float lw_smem[(sizeof(LegWork<float>) / 4) * 128];
+  LegWork<float> lw;
+  LegOut<float> o = phase_a(M, leg, B, L, lp, act, lw);
+  {
+    const float* src = reinterpret_cast<const float*>(&lw);
+#pragma unroll
+    for (int f = 0; f < (int)(sizeof(LegWork<float>) / 4); ++f) lw_smem[f * 128 + threadIdx.x] = src[f];
+  }
+  qsum_out(o);
+  SV<float> a0 = phase_b(M, bp, o, B);
+  LegWork<float> lw2;
+  {
+    float* dst = reinterpret_cast<float*>(&lw2);
+#pragma unroll
+    for (int f = 0; f < (int)(sizeof(LegWork<float>) / 4); ++f) dst[f] = lw_smem[f * 128 + threadIdx.x];
+  }
+  phase_c(M, leg, a0, lw2, L);
+}
+
 template <bool TRACE>
 __device__ __forceinline__ void rollout_group(const DevModel& M, const WinView& win, const float* th13,
                                               int group, float* partial9, float* trace,
@@ -99,13 +126,7 @@ __device__ __forceinline__ void rollout_group(const DevModel& M, const WinView& 
     float act[3];
     const float* ap = win.act + ((size_t)h * W + w) * 12 + 3 * leg;
     act[0] = __ldg(ap); act[1] = __ldg(ap + 1); act[2] = __ldg(ap + 2);
-    for (int s = 0; s < dec; ++s) {
-      LegWork<float> lw;
-      LegOut<float> o = phase_a(M, leg, B, L, lp, act, lw);
-      qsum_out(o);
-      SV<float> a0 = phase_b(M, bp, o, B);
-      phase_c(M, leg, a0, lw, L);
-    }
+    for (int s = 0; s < dec; ++s) substep(M, leg, B, L, bp, lp, act);
     if (TRACE && active) {
       float* tp = trace + ((size_t)w * H + h) * SPI_STATE_DIM;
       if (leg == 0) {

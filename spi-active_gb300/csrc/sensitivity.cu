@@ -10,6 +10,7 @@
 // spi_fisher: F_n = sum_w J_w^T diag(q) J_w (FP32 accumulation), log det(F_n + eps I) and
 // trace(F_n) in FP64 -- the active-exploration scores (trace is the reference's objective,
 // spigym/envs/sysid/active_sysid_openloop.py:402-426; log det the D-optimal one).
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -139,6 +140,62 @@ __global__ void fisher_kernel(const float* __restrict__ J, int N, int W, int K, 
   }
 }
 
+// F[n] = sum_w J^T diag(q) J on tensor cores: one warp per sample, BF16 operands, FP32
+// accumulation, mma.sync m16n8k16 (A = (Q^1/2 J)^T as a 16 x 16 row-major tile, B = Q^1/2 J as a
+// 16 x 8 column-major tile, two n-tiles cover the 16 padded parameters). Rows of J are consumed
+// 16 at a time; rows past W * 37 and parameters past K are zero.
+__device__ __forceinline__ unsigned pack_bf16(float lo, float hi) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<unsigned*>(&v);
+}
+__device__ __forceinline__ float jq(const float* __restrict__ Jn, const float* __restrict__ q, int rows, int K,
+                                    int r, int p) {
+  if (r >= rows || p >= K) return 0.f;
+  const float w = q ? sqrtf(q[r % SPI_STATE_DIM]) : 1.f;
+  return w * Jn[(size_t)r * K + p];
+}
+__global__ void fisher_mma_kernel(const float* __restrict__ J, int N, int W, int K, const float* __restrict__ q,
+                                  float* __restrict__ F) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= N) return;                        // uniform per warp
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const float* Jn = J + (size_t)warp * W * SPI_STATE_DIM * K;
+  const int rows = W * SPI_STATE_DIM;
+  float c0[4] = {0.f, 0.f, 0.f, 0.f}, c1[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int k0 = 0; k0 < rows; k0 += 16) {
+    // A[m][k] = Jq[k0 + k][m]: rows m = g, g + 8; cols k = 2t, 2t + 1, 2t + 8, 2t + 9
+    const unsigned a0 = pack_bf16(jq(Jn, q, rows, K, k0 + 2 * t, g), jq(Jn, q, rows, K, k0 + 2 * t + 1, g));
+    const unsigned a1 = pack_bf16(jq(Jn, q, rows, K, k0 + 2 * t, g + 8), jq(Jn, q, rows, K, k0 + 2 * t + 1, g + 8));
+    const unsigned a2 = pack_bf16(jq(Jn, q, rows, K, k0 + 2 * t + 8, g), jq(Jn, q, rows, K, k0 + 2 * t + 9, g));
+    const unsigned a3 = pack_bf16(jq(Jn, q, rows, K, k0 + 2 * t + 8, g + 8),
+                                  jq(Jn, q, rows, K, k0 + 2 * t + 9, g + 8));
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt) {
+      // B[k][n] = Jq[k0 + k][8 nt + n]: k = 2t, 2t + 1 (b0) and 2t + 8, 2t + 9 (b1); n = g
+      const int n = 8 * nt + g;
+      const unsigned b0 = pack_bf16(jq(Jn, q, rows, K, k0 + 2 * t, n), jq(Jn, q, rows, K, k0 + 2 * t + 1, n));
+      const unsigned b1 = pack_bf16(jq(Jn, q, rows, K, k0 + 2 * t + 8, n), jq(Jn, q, rows, K, k0 + 2 * t + 9, n));
+      float* c = nt ? c1 : c0;
+      asm volatile(
+          "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+          "{%0, %1, %2, %3};\n"
+          : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+          : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+    }
+  }
+  // D fragment: rows g and g + 8, cols 2t and 2t + 1 of each n-tile
+  float* Fn = F + (size_t)warp * K * K;
+#pragma unroll
+  for (int nt = 0; nt < 2; ++nt) {
+    const float* c = nt ? c1 : c0;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int m = g + (e >= 2 ? 8 : 0), n = 8 * nt + 2 * t + (e & 1);
+      if (m < K && n < K) Fn[m * K + n] = c[e];
+    }
+  }
+}
+
 // log det(F + eps I) by FP64 Cholesky, and trace(F); one thread per sample.
 __global__ void logdet_kernel(const float* __restrict__ F, int N, int K, double eps, double* __restrict__ logdet,
                               double* __restrict__ trace) {
@@ -192,10 +249,18 @@ int spi_sensitivity(spi_engine* e, const float* theta, int N, const int32_t* par
 
 int spi_fisher(const float* J, int N, int W, int K, const float* state_weight, double eps, float* F, double* logdet,
                double* trace, void* stream) {
+  return spi_fisher_ex(J, N, W, K, state_weight, eps, 0, F, logdet, trace, stream);
+}
+
+int spi_fisher_ex(const float* J, int N, int W, int K, const float* state_weight, double eps, int tensor_cores,
+                  float* F, double* logdet, double* trace, void* stream) {
   if (!J || !F || N <= 0 || W <= 0 || K < 1 || K > SPI_THETA_DIM)
     return set_error(SPI_EINVAL, "spi_fisher: bad argument");
   cudaStream_t s = (cudaStream_t)stream;
-  fisher_kernel<<<N, 128, 0, s>>>(J, N, W, K, state_weight, F);
+  if (tensor_cores)
+    fisher_mma_kernel<<<(N + 3) / 4, 128, 0, s>>>(J, N, W, K, state_weight, F);
+  else
+    fisher_kernel<<<N, 128, 0, s>>>(J, N, W, K, state_weight, F);
   if (logdet || trace) logdet_kernel<<<(N + 127) / 128, 128, 0, s>>>(F, N, K, eps, logdet, trace);
   cudaError_t ce = cudaGetLastError();
   return ce == cudaSuccess ? SPI_OK : cuda_error(ce, "spi_fisher");

@@ -74,7 +74,8 @@ __global__ void srv_fill(float* p, float v, int n) {
 }
 
 // Persistent rollout over the work items of every active slot.
-__global__ void __launch_bounds__(128, 3) server_rollout_kernel(const DevModel* __restrict__ model,
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) server_rollout_kernel(const DevModel* __restrict__ model,
                                                              const SlotDesc* __restrict__ slots,
                                                              const int* __restrict__ order,
                                                              const TickInfo* __restrict__ info,
@@ -165,6 +166,7 @@ struct spi_server {
   cudaGraphExec_t graph = nullptr;
   int grid = 0, ctas_per_sm = 0, items_per_claim = 1;
   long long max_items = 0;         // admission cap on work items per tick (0: none)
+  int min_blocks = 3;              // rollout kernel occupancy variant
   int cost_mode = 1;
   float sq_w[6] = {10.f, 5.f, 0.1f, 0.1f, 1.f, 0.01f};
   long long ticks = 0;
@@ -195,8 +197,12 @@ int enqueue_tick(spi_server* s) {
   cudaError_t ce = cudaMemsetAsync(s->d_counter, 0, sizeof(unsigned long long), s->stream);
   if (ce != cudaSuccess) return cuda_error(ce, "tick: reset counter");
   cem_sample_kernel<<<dim3(rows, s->max_slots), 128, 0, s->stream>>>(s->d_cem);
-  server_rollout_kernel<<<s->grid, 128, 0, s->stream>>>(s->d_model, s->d_slots, s->d_order, s->d_info,
-                                                        s->d_counter, s->d_bad);
+  if (s->min_blocks == 4)
+    server_rollout_kernel<4><<<s->grid, 128, 0, s->stream>>>(s->d_model, s->d_slots, s->d_order, s->d_info,
+                                                             s->d_counter, s->d_bad);
+  else
+    server_rollout_kernel<3><<<s->grid, 128, 0, s->stream>>>(s->d_model, s->d_slots, s->d_order, s->d_info,
+                                                             s->d_counter, s->d_bad);
   const float* w = s->sq_w;
   server_finalize_kernel<<<dim3(rows, s->max_slots), 128, 0, s->stream>>>(s->d_slots, s->cost_mode, w[0], w[1],
                                                                           w[2], w[3], w[4], w[5]);
@@ -229,7 +235,9 @@ int resize_grid(spi_server* s) {
   int dev = 0, sms = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaError_t ce = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_kernel, 128, 0);
+  cudaError_t ce = s->min_blocks == 4
+                       ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_kernel<4>, 128, 0)
+                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_kernel<3>, 128, 0);
   if (ce != cudaSuccess) return cuda_error(ce, "server: occupancy");
   const int per = s->ctas_per_sm > 0 ? std::min(s->ctas_per_sm, std::max(occ, 1)) : std::max(occ, 1);
   s->grid = sms * per;
@@ -329,6 +337,14 @@ int spi_server_config(spi_server* s, int ctas_per_sm, int items_per_claim) {
     return set_error(SPI_EINVAL, "spi_server_config: ctas_per_sm %d items_per_claim %d", ctas_per_sm, items_per_claim);
   s->ctas_per_sm = ctas_per_sm;
   s->items_per_claim = items_per_claim;
+  return resize_grid(s);
+}
+
+int spi_server_set_kernel_config(spi_server* s, int min_blocks) {
+  if (!s) return set_error(SPI_EINVAL, "null server");
+  if (min_blocks != 3 && min_blocks != 4)
+    return set_error(SPI_EINVAL, "spi_server_set_kernel_config: min_blocks %d not 3 or 4", min_blocks);
+  s->min_blocks = min_blocks;
   return resize_grid(s);
 }
 

@@ -49,13 +49,7 @@ __global__ void __launch_bounds__(128) step_kernel(const DevModel* __restrict__ 
   for (int h = 0; h < steps; ++h) {
     const float* ap = actions + ((size_t)row * steps + h) * 12 + 3 * leg;
     float act[3] = {ap[0], ap[1], ap[2]};
-    for (int s = 0; s < M.decimation; ++s) {
-      LegWork<float> lw;
-      LegOut<float> o = phase_a(M, leg, Bs, L, lp, act, lw);
-      qsum_out(o);
-      SV<float> a0 = phase_b(M, bp, o, Bs);
-      phase_c(M, leg, a0, lw, L);
-    }
+    for (int s = 0; s < M.decimation; ++s) substep(M, leg, Bs, L, bp, lp, act);
   }
   if (!active) return;
   if (leg == 0) {

@@ -45,6 +45,8 @@ ENGINE_API = {
     "spi_sensitivity": (c_int, [c_void_p, c_void_p, c_int, POINTER(ctypes.c_int32), c_int, c_void_p, c_void_p]),
     "spi_fisher": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_double, c_void_p, c_void_p, c_void_p,
                            c_void_p]),
+    "spi_fisher_ex": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_double, c_int, c_void_p, c_void_p,
+                              c_void_p, c_void_p]),
     "spi_probe_fp32_peak": (c_int, [POINTER(c_double)]),
     "spi_eval_windows_noalloc": (c_int, [POINTER(SpiRobot), c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int,
                                          c_float, c_void_p, c_int, c_int, POINTER(c_float), c_void_p, c_void_p,

@@ -29,8 +29,11 @@ def sensitivities(engine, theta, param_ids):
     return J, xH
 
 
-def fisher(J, state_weight=None, eps=1e-9, stream=None):
-    """F [N, K, K] (FP32 accumulation), log det(F + eps I) and trace(F) (FP64) from J [N, W, 37, K]."""
+def fisher(J, state_weight=None, eps=1e-9, stream=None, tensor_cores=False):
+    """F [N, K, K], log det(F + eps I) and trace(F) (FP64) from J [N, W, 37, K].
+
+    tensor_cores: accumulate J^T Q J on the tensor cores (BF16 operands, FP32 accumulation)
+    instead of FP32 on the CUDA cores."""
     J = J.contiguous()
     N, W, S, K = J.shape
     F = torch.empty((N, K, K), device=J.device)
@@ -40,9 +43,9 @@ def fisher(J, state_weight=None, eps=1e-9, stream=None):
     if state_weight is not None:
         q = torch.as_tensor(state_weight, dtype=torch.float32, device=J.device).contiguous()
     s = stream or torch.cuda.current_stream(J.device)
-    _lib.check(_lib.engine_lib().spi_fisher(J.data_ptr(), N, W, K, q.data_ptr() if q is not None else None,
-                                            float(eps), F.data_ptr(), logdet.data_ptr(), trace.data_ptr(),
-                                            ctypes.c_void_p(s.cuda_stream)))
+    _lib.check(_lib.engine_lib().spi_fisher_ex(J.data_ptr(), N, W, K, q.data_ptr() if q is not None else None,
+                                               float(eps), int(bool(tensor_cores)), F.data_ptr(), logdet.data_ptr(),
+                                               trace.data_ptr(), ctypes.c_void_p(s.cuda_stream)))
     return F, logdet, trace
 
 
@@ -91,7 +94,7 @@ def multisine_actions(n_cand, T, control_dt, action_scale, n_comp=3, amp=(0.05, 
 
 
 def score_excitations(engine, theta, actions, windows_per_cand=8, horizon=20, settle=100, param_ids=None,
-                      sq_weights=(10.0, 5.0, 0.1, 0.1, 1.0, 0.01), eps=1e-9):
+                      sq_weights=(10.0, 5.0, 0.1, 0.1, 1.0, 0.01), eps=1e-9, tensor_cores=True):
     """Fisher scores of candidate excitations at theta.
 
     actions [n_cand, settle + windows_per_cand * horizon, 12]. Each candidate is rolled from a
@@ -113,6 +116,6 @@ def score_excitations(engine, theta, actions, windows_per_cand=8, horizon=20, se
     engine.load_windows(init, act, init)
     J, _ = sensitivities(engine, torch.from_numpy(theta), param_ids)          # [1, n*wpc, 37, K]
     J = J.reshape(n, windows_per_cand, STATE_DIM, len(param_ids))
-    F, logdet, trace = fisher(J, block_weights(sq_weights), eps)
+    F, logdet, trace = fisher(J, block_weights(sq_weights), eps, tensor_cores=tensor_cores)
     ld = logdet.cpu().numpy()
     return {"logdet": ld, "trace": trace.cpu().numpy(), "best": int(np.argmax(ld)), "F": F, "J": J}

@@ -44,6 +44,7 @@ _API = {
                                         ctypes.POINTER(ctypes.c_size_t)]),
     "spi_server_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "spi_server_wait": (ctypes.c_int, [ctypes.c_void_p]),
+    "spi_server_set_kernel_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "spi_server_set_work_cap": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong]),
 }
 
@@ -142,6 +143,9 @@ class Server:
                         "best_theta": np.array(r.best_theta[:], np.float32), "mu": np.array(r.mu[:r.dim]),
                         "status": r.status, "latency_s": now - self.submitted.pop(r.job_id, now)})
         return out
+
+    def set_kernel_config(self, min_blocks):
+        _lib.check(self.lib.spi_server_set_kernel_config(self._h, int(min_blocks)))
 
     def set_work_cap(self, max_items):
         _lib.check(self.lib.spi_server_set_work_cap(self._h, int(max_items)))

@@ -35,6 +35,7 @@ class JobSpec:
     seed: int
     theta_true: np.ndarray
     arrival: float = 0.0
+    fisher: bool = False      # also score candidate excitations at the identified theta
 
     @property
     def rollout_steps(self) -> int:
@@ -60,12 +61,35 @@ def small_specs(n_jobs, seed=0, iterations=30):
     return c2_specs(n_jobs, seed=seed, iterations=iterations, pop=(64, 512), windows=(8, 64), horizon=(5, 20))
 
 
-def poisson_arrivals(specs, rate, seed=0):
+def poisson_arrivals(specs, rate, seed=0, fisher_frac=0.0):
+    """Poisson arrival times at `rate` jobs/s; a `fisher_frac` share of jobs also asks for an
+    excitation score."""
     rng = np.random.default_rng(seed)
     t = np.cumsum(rng.exponential(1.0 / rate, len(specs)))
     for s, a in zip(specs, t):
         s.arrival = float(a)
+        s.fisher = bool(rng.random() < fisher_frac)
     return specs
+
+
+FISHER_CANDIDATES, FISHER_WINDOWS, FISHER_H = 32, 4, 20
+
+
+class FisherScorer:
+    """Excitation scoring at an identified theta (the Fisher request of a job)."""
+
+    def __init__(self, cfg: SimConfig | None = None, device=None):
+        from .sensitivity import multisine_actions
+        self.engine = Engine(cfg, device=device)
+        c = self.engine.cfg
+        self.actions, _ = multisine_actions(FISHER_CANDIDATES, FISHER_WINDOWS * FISHER_H, c.control_dt,
+                                            c.action_scale, seed=11, settle=100)
+
+    def score(self, theta):
+        from .sensitivity import score_excitations
+        r = score_excitations(self.engine, theta, self.actions, windows_per_cand=FISHER_WINDOWS, horizon=FISHER_H,
+                              settle=100)
+        return {"best_candidate": r["best"], "logdet": float(r["logdet"][r["best"]])}
 
 
 class WindowBank:
@@ -122,6 +146,8 @@ def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=
         init, act, tgt = bank.get(s)
         jobs[s.job_id] = (Server.make_job(init, act, tgt, _cem_cfg(s), s.iterations), (init, act, tgt))
     pending = sorted(specs, key=lambda s: s.arrival)
+    scorer = FisherScorer(cfg, device=bank.engine.device) if any(s.fisher for s in specs) else None
+    by_id = {s.job_id: s for s in specs}
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     done, lat, results = 0, {}, {}
@@ -140,8 +166,9 @@ def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=
             if qi < len(pending) and realtime:
                 time.sleep(max(0.0, min(pending[qi].arrival - (time.perf_counter() - t0), 0.002)))
         for r in server.poll():
-            spec = specs[r["job_id"]] if specs[r["job_id"]].job_id == r["job_id"] else \
-                next(s for s in specs if s.job_id == r["job_id"])
+            spec = by_id[r["job_id"]]
+            if spec.fisher:
+                r["fisher"] = scorer.score(r["best_theta"])
             lat[r["job_id"]] = time.perf_counter() - t0 - spec.arrival
             results[r["job_id"]] = r
             done += 1
@@ -153,6 +180,7 @@ def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=
 def run_plain(specs, bank: WindowBank, cfg: SimConfig | None = None, graph=True):
     """One job at a time through the single-job engine, in arrival order (FIFO)."""
     eng = Engine(cfg, device=bank.engine.device)
+    scorer = FisherScorer(cfg, device=bank.engine.device) if any(s.fisher for s in specs) else None
     order = sorted(specs, key=lambda s: s.arrival)
     for s in order:
         bank.get(s)
@@ -170,6 +198,8 @@ def run_plain(specs, bank: WindowBank, cfg: SimConfig | None = None, graph=True)
                   job_id=s.job_id)
         cem.run(s.iterations, graph=graph)
         r = cem.read()
+        if s.fisher:
+            r["fisher"] = scorer.score(r["best_theta"])
         lat[s.job_id] = time.perf_counter() - t0 - s.arrival
         results[s.job_id] = r
     wall = time.perf_counter() - t0

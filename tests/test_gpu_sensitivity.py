@@ -74,6 +74,19 @@ def test_fisher_and_logdet_match_fp64(case):
     np.testing.assert_allclose(trace.cpu().numpy(), np.trace(Fr, axis1=1, axis2=2), rtol=1e-5)
 
 
+def test_fisher_on_tensor_cores(case):
+    """BF16 operands, FP32 accumulation: within 1e-2 of the FP64 reduction (BF16 has 8 mantissa bits)."""
+    from spi_gb300.sensitivity import block_weights, fisher, sensitivities
+    e, x0, acts, target, theta = case
+    J, _ = sensitivities(e, torch.from_numpy(theta.astype(np.float32)), list(range(13)))
+    q = block_weights((10.0, 5.0, 0.1, 0.1, 1.0, 0.01))
+    F, logdet, trace = fisher(J, q, eps=1e-9, tensor_cores=True)
+    Fr = ofi.fisher_matrix(J.cpu().numpy().astype(np.float64), q.astype(np.float64))
+    err = np.abs(F.cpu().numpy() - Fr).max(axis=(1, 2)) / np.abs(Fr).max(axis=(1, 2))
+    assert err.max() <= 1e-2, err
+    np.testing.assert_allclose(trace.cpu().numpy(), np.trace(Fr, axis1=1, axis2=2), rtol=1e-2)
+
+
 def test_window_cost_autograd_matches_fd(case):
     from spi_gb300.sensitivity import WindowCost, block_weights
     e, x0, acts, target, theta = case

@@ -38,7 +38,9 @@ def test_step_states_matches_trace_and_oracle(built):
     sim2.step(torch.from_numpy(actions), control_steps=6)
     _, _, tr = e.evaluate(torch.from_numpy(th[:1]), trace=True)
     torch.cuda.synchronize()
-    assert torch.equal(sim2.state, tr[0, :, -1])
+    # the same substep code in two kernels: rounding may differ at the ulp level where the
+    # compiler fuses multiply-adds differently, so the check is a tolerance, not equality
+    assert state_error(sim2.state.cpu().numpy(), tr[0, :, -1].cpu().numpy()) <= 1e-5
 
 
 def test_params_dict_mapping(built):
