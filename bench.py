@@ -17,6 +17,7 @@ same workload. Under torchrun (N > 1) every rank runs an independent replica job
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import subprocess
@@ -180,6 +181,14 @@ def served_vs_plain(specs, realtime, cfg=None):
     for name, r in (("served", served), ("plain", plain)):
         out[name] = {k: v for k, v in r.items() if k != "results"}
     out["speedup_rollout_steps"] = served["rollout_steps_per_s"] / plain["rollout_steps_per_s"]
+    # Correctness at the 1e-4 relative cost bar: one CEM iteration per job, served and plain. Both
+    # paths score the same seeded prior population, so their best costs are comparable directly.
+    one = [dataclasses.replace(s, iterations=1, arrival=0.0, fisher=False) for s in specs]
+    s1 = run_served(one, bank, cfg, realtime=False)["results"]
+    p1 = run_plain(one, bank, cfg)["results"]
+    errs = [abs(s1[s.job_id]["best_cost"] - p1[s.job_id]["best_cost"]) / max(abs(p1[s.job_id]["best_cost"]), 1e-30)
+            for s in one]
+    out["max_rel_cost_err_first_iteration"] = float(max(errs))
     # The served and plain kernels are separate compilations of the same rollout; ulp-level
     # rounding differences change a CEM's elite set, after which the two searches part ways.
     # The ratio of their final best costs therefore checks that both converge equally well.
@@ -340,7 +349,8 @@ def run_ours(args):
             "traffic_note": "dram read+write bytes per launch from ncu on 1024 theta x the same 256 windows "
                             "(profiles/rollout_kernel_1024x256xH20_after_sparse.md); the window set is read once "
                             "and theta / partials stay in L2, so traffic does not scale with theta",
-            "kernel": "rollout_kernel (+finalize_costs)", "kernel_ms": kmean,
+            "kernel": ("rollout_lane_kernel" if variant.startswith("lane") else "rollout_kernel") + " (+finalize_costs)",
+            "kernel_ms": kmean,
             "flops_per_rollout_step": fl,
             "peak_source": "measured FP32 FMA-loop probe on this GPU (no FP32 entry in MEASURED_PEAKS.json)"}
     if rank != 0:
@@ -354,7 +364,7 @@ def run_ours(args):
                        "n_params": 13, "elite_frac": C1["elite_frac"],
                        "step": "one CEM iteration (rollouts + cost + refit + resample)",
                        "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{ws}",
-                       "kernel_variant": {"ctas_per_sm_target": variant, "tuning_ms": variant_ms}},
+                       "kernel_variant": {"chosen": variant, "tuning_ms": variant_ms}},
             "roofline": roof, "e2e": e2e, "gpu_launches": cem.launches_per_step * args.steps,
             "wall_s": wall, "nonfinite_rollouts": n_bad, "clocks": clocks.summary(),
             "cem": {"best_cost": cem.best_cost(), "theta_err": cem.theta_error(theta_true)}}

@@ -114,8 +114,18 @@ int spi_set_theta(spi_engine* e, const float* theta, int N);
 int spi_set_cost(spi_engine* e, int mode, const float* sq_weights);
 
 /* Rollout-kernel variant: the register allocator targets min_blocks CTAs of 128 threads per
- * SM (3: 168 registers, no spills; 4: 128 registers; 5: 96 registers). Same results. */
+ * SM (2: 255 registers; 3: 168; 4: 128; 5: 96; the quad layout takes 3..5, the lane layout
+ * 2..3). Same equations; results within FP32 rounding of each other. */
 int spi_set_kernel_config(spi_engine* e, int min_blocks);
+
+/* Rollout-kernel lane layout. SPI_LAYOUT_QUAD: four lanes per rollout, one leg each, the base
+ * solved on all four. SPI_LAYOUT_LANE: one lane per rollout through all four legs, the model
+ * in the kernel's parameter block, 69 KB of shared memory per 128-thread CTA (so at most 3
+ * CTAs per SM: min_blocks 2 or 3, larger values act as 3). Same equations, results within
+ * FP32 rounding of each other; spi_run_trace always uses the quad layout. */
+#define SPI_LAYOUT_QUAD 0
+#define SPI_LAYOUT_LANE 1
+int spi_set_kernel_layout(spi_engine* e, int layout);
 
 /* Roll every (theta, window) pair H control steps and reduce the windowed cost. Async. */
 int spi_run(spi_engine* e);

@@ -333,6 +333,11 @@ template <class T> struct LegOut { Art<T> I; SV<T> p; };            // leg contr
 template <class T> struct LegWork {                                 // phase A -> phase C
   SV<T> U[3], cb[3];
   T invD[3], u[3], c[3], s[3];
+  // phase A hands its results over through these (a kernel may store them elsewhere, e.g.
+  // straight to shared memory, with a type that has the same three members)
+  SPI_INL void put_cs(int k, T cc, T ss) { c[k] = cc; s[k] = ss; }
+  SPI_INL void put_cb(int k, const SV<T>& v) { cb[k] = v; }
+  SPI_INL void put_U(int k, const SV<T>& Uk, T invDk, T uk) { U[k] = Uk; invD[k] = invDk; u[k] = uk; }
 };
 
 template <class T> SPI_INL M3<T> quat_to_R(T x, T y, T z, T w) {
@@ -435,9 +440,9 @@ template <int AX, class T> SPI_INL SV<T> vel_product(const SV<T>& v, T qd) {
 }
 
 // One ABA backward step of joint k (axis AX): project out the joint, move to the parent.
-template <int AX, int RM, class T> SPI_INL void aba_back(Art<T>& IA, SV<T>& pA, const SV<T>& cb, T tau, T arm,
-                                                 T c, T s, V3<T> r, LegWork<T>& W, int k,
-                                                 Art<T>* Iout, SV<T>* pout) {
+template <int AX, int RM, class T, class WK>
+SPI_INL void aba_back(Art<T>& IA, SV<T>& pA, const SV<T>& cb, T tau, T arm, T c, T s, V3<T> r, WK& W, int k,
+                      Art<T>* Iout, SV<T>* pout) {
   SV<T> U;
   U.w = col(IA.A, AX);
   U.v = row(IA.B, AX);
@@ -459,7 +464,7 @@ template <int AX, int RM, class T> SPI_INL void aba_back(Art<T>& IA, SV<T>& pA, 
   T uD = u * invD;
   pa.w = pA.w + pa.w + uD * U.w;
   pa.v = pA.v + pa.v + uD * U.v;
-  W.U[k] = U; W.invD[k] = invD; W.u[k] = u;
+  W.put_U(k, U, invD, u);
   *Iout = art_to_parent<AX, RM>(Ia, c, s, r);
   *pout = force_to_parent<AX, RM>(pa, c, s, r);
 }
@@ -467,41 +472,42 @@ template <int AX, int RM, class T> SPI_INL void aba_back(Art<T>& IA, SV<T>& pA, 
 // ---------------------------------------------------------------------------
 // Phase A: everything of one leg (and two base corners) up to its base contribution.
 // ---------------------------------------------------------------------------
-template <class T>
+template <class T, class WK>
 SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
-                          const LegParams<T>& P, const T act[3], LegWork<T>& W) {
-  T tau[3];
+                          const LegParams<T>& P, const T act[3], WK& W) {
+  T tau[3], C[3], S[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     tau[k] = motor_torque(M, P, k, leg, act[k], L.q[k], L.qd[k]);
-    m_sincos(L.q[k], &W.s[k], &W.c[k]);
+    m_sincos(L.q[k], &S[k], &C[k]);
+    W.put_cs(k, C[k], S[k]);
   }
   V3<T> r0 = leg_org<T>(M, 0, leg), r1 = leg_org<T>(M, 1, leg), r2 = leg_org<T>(M, 2, leg);
   // body velocities (body coordinates) and velocity-product accelerations
-  SV<T> v0 = motion_to_child<0>(B.nu, W.c[0], W.s[0], r0); v0.w.x = v0.w.x + L.qd[0];
-  SV<T> v1 = motion_to_child<1, 2>(v0, W.c[1], W.s[1], r1);   v1.w.y = v1.w.y + L.qd[1];
-  SV<T> v2 = motion_to_child<1, 4>(v1, W.c[2], W.s[2], r2);   v2.w.y = v2.w.y + L.qd[2];
-  W.cb[0] = vel_product<0>(v0, L.qd[0]);
-  W.cb[1] = vel_product<1>(v1, L.qd[1]);
-  W.cb[2] = vel_product<1>(v2, L.qd[2]);
+  SV<T> v0 = motion_to_child<0>(B.nu, C[0], S[0], r0); v0.w.x = v0.w.x + L.qd[0];
+  SV<T> v1 = motion_to_child<1, 2>(v0, C[1], S[1], r1);   v1.w.y = v1.w.y + L.qd[1];
+  SV<T> v2 = motion_to_child<1, 4>(v1, C[2], S[2], r2);   v2.w.y = v2.w.y + L.qd[2];
+  const SV<T> cb0 = vel_product<0>(v0, L.qd[0]), cb1 = vel_product<1>(v1, L.qd[1]),
+              cb2 = vel_product<1>(v2, L.qd[2]);
+  W.put_cb(0, cb0); W.put_cb(1, cb1); W.put_cb(2, cb2);
   // foot: position and velocity, calf -> thigh -> hip -> base -> world
   V3<T> fc = v3(T(M.foot[0]), T(M.foot[1]), T(M.foot[2]));
   V3<T> vf = v2.v + cross(v2.w, fc);
-  V3<T> pf = rot<1>(W.c[2], W.s[2], fc) + r2;
-  vf = rot<1>(W.c[2], W.s[2], vf);
-  pf = rot<1>(W.c[1], W.s[1], pf) + r1;
-  vf = rot<1>(W.c[1], W.s[1], vf);
-  pf = rot<0>(W.c[0], W.s[0], pf) + r0;
-  vf = rot<0>(W.c[0], W.s[0], vf);
+  V3<T> pf = rot<1>(C[2], S[2], fc) + r2;
+  vf = rot<1>(C[2], S[2], vf);
+  pf = rot<1>(C[1], S[1], pf) + r1;
+  vf = rot<1>(C[1], S[1], vf);
+  pf = rot<0>(C[0], S[0], pf) + r0;
+  vf = rot<0>(C[0], S[0], vf);
   T mimp;
   V3<T> F = contact_force(M, T(M.foot_r), B.p.z + dot(row(B.R, 2), pf), mul(B.R, vf), &mimp);
   // the implicit point mass acts on the true acceleration while the ABA runs in the
   // gravity-shifted frame: its share of the shift enters as a force mimp*g upwards
   F.z = F.z + mimp * T(M.g);
   V3<T> Fc = mulT(B.R, F);
-  Fc = rotT<0>(W.c[0], W.s[0], Fc);
-  Fc = rotT<1>(W.c[1], W.s[1], Fc);
-  Fc = rotT<1>(W.c[2], W.s[2], Fc);
+  Fc = rotT<0>(C[0], S[0], Fc);
+  Fc = rotT<1>(C[1], S[1], Fc);
+  Fc = rotT<1>(C[2], S[2], Fc);
   // ABA backward pass: calf -> thigh -> hip -> base
   Art<T> IA = leg_rigid<T>(M, 2, leg);
   add_point_mass(IA, mimp, fc);
@@ -509,14 +515,14 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
   pA.w = pA.w - cross(fc, Fc);
   pA.v = pA.v - Fc;
   Art<T> Ip; SV<T> pp;
-  aba_back<1, 4>(IA, pA, W.cb[2], tau[2], P.arm, W.c[2], W.s[2], r2, W, 2, &Ip, &pp);
+  aba_back<1, 4>(IA, pA, cb2, tau[2], P.arm, C[2], S[2], r2, W, 2, &Ip, &pp);
   IA = leg_rigid<T>(M, 1, leg); add_to(IA, Ip);
   pA = leg_bias(M, 1, leg, v1); pA.w = pA.w + pp.w; pA.v = pA.v + pp.v;
-  aba_back<1, 2>(IA, pA, W.cb[1], tau[1], P.arm, W.c[1], W.s[1], r1, W, 1, &Ip, &pp);
+  aba_back<1, 2>(IA, pA, cb1, tau[1], P.arm, C[1], S[1], r1, W, 1, &Ip, &pp);
   IA = leg_rigid<T>(M, 0, leg); add_to(IA, Ip);
   pA = leg_bias(M, 0, leg, v0); pA.w = pA.w + pp.w; pA.v = pA.v + pp.v;
   LegOut<T> out;
-  aba_back<0, 7>(IA, pA, W.cb[0], tau[0], P.arm, W.c[0], W.s[0], r0, W, 0, &out.I, &out.p);
+  aba_back<0, 7>(IA, pA, cb0, tau[0], P.arm, C[0], S[0], r0, W, 0, &out.I, &out.p);
   // two of the eight base-box corners; a corner can only reach the ground when the base origin
   // is lower than the box's half-diagonal, so a warp whose rollouts are all higher skips them
   // (a corner off the ground adds exactly zero force and zero implicit mass)

@@ -8,6 +8,7 @@
 #include "common.h"
 #include "model.h"
 #include "rollout.cuh"
+#include "rollout_lane.cuh"
 #include "engine_impl.h"
 
 using namespace spi;
@@ -66,7 +67,16 @@ int spi::run_impl(spi_engine* e, float* trace) {
   const long long warps = (long long)e->N * G;
   const unsigned grid = blocks_for(warps, 4);
   unsigned long long* bad = (unsigned long long*)e->bad.p;
-  if (trace)
+  if (!trace && e->layout == SPI_LAYOUT_LANE) {
+    const long long lwarps = (long long)e->N * ((e->W + 31) / 32);
+    const unsigned lgrid = blocks_for(lwarps, 4);
+    if (e->min_blocks <= 2)
+      rollout_lane_kernel<2><<<lgrid, 128, kLaneParkBytes, e->stream>>>(e->host_model, win, e->theta.f(), e->N, G,
+                                                                        e->partial.f(), bad);
+    else
+      rollout_lane_kernel<3><<<lgrid, 128, kLaneParkBytes, e->stream>>>(e->host_model, win, e->theta.f(), e->N, G,
+                                                                        e->partial.f(), bad);
+  } else if (trace)
     rollout_kernel<true, 3><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
                                                          e->partial.f(), trace, bad);
   else if (e->min_blocks == 4)
@@ -176,9 +186,30 @@ int spi_set_theta(spi_engine* e, const float* theta, int N) {
 
 int spi_set_kernel_config(spi_engine* e, int min_blocks) {
   if (!e) return set_error(SPI_EINVAL, "null engine");
-  if (min_blocks < 3 || min_blocks > 5)
-    return set_error(SPI_EINVAL, "spi_set_kernel_config: min_blocks %d outside [3, 5]", min_blocks);
+  const int lo = e->layout == SPI_LAYOUT_LANE ? 2 : 3;
+  if (min_blocks < lo || min_blocks > 5)
+    return set_error(SPI_EINVAL, "spi_set_kernel_config: min_blocks %d outside [%d, 5]", min_blocks, lo);
   e->min_blocks = min_blocks;
+  if (e->graph_exec) { cudaGraphExecDestroy(e->graph_exec); e->graph_exec = nullptr; }
+  return SPI_OK;
+}
+
+int spi_set_kernel_layout(spi_engine* e, int layout) {
+  if (!e) return set_error(SPI_EINVAL, "null engine");
+  if (layout != SPI_LAYOUT_QUAD && layout != SPI_LAYOUT_LANE)
+    return set_error(SPI_EINVAL, "spi_set_kernel_layout: layout %d not 0/1", layout);
+  if (layout == SPI_LAYOUT_LANE) {
+    // the parking area is above the 48 KB default for dynamic shared memory
+    cudaError_t ce = cudaFuncSetAttribute(rollout_lane_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          kLaneParkBytes);
+    if (ce == cudaSuccess)
+      ce = cudaFuncSetAttribute(rollout_lane_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                kLaneParkBytes);
+    if (ce != cudaSuccess) return cuda_error(ce, "spi_set_kernel_layout: shared-memory attribute");
+  } else if (e->min_blocks < 3) {
+    e->min_blocks = 3;
+  }
+  e->layout = layout;
   if (e->graph_exec) { cudaGraphExecDestroy(e->graph_exec); e->graph_exec = nullptr; }
   return SPI_OK;
 }

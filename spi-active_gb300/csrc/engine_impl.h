@@ -22,6 +22,7 @@ struct spi_engine {
   float sq_w[6] = {10.f, 5.f, 0.1f, 0.1f, 1.f, 0.01f};
   bool ran = false;
   int min_blocks = 3;                      // rollout kernel occupancy variant
+  int layout = 0;                          // SPI_LAYOUT_QUAD / SPI_LAYOUT_LANE
   // CEM
   spi::DeviceBuf cem;                      // one CemState
   bool cem_ready = false;

@@ -64,30 +64,96 @@ __device__ __forceinline__ void load_model_smem(DevModel* dst, const DevModel* _
 // Roll one warp's eight windows for theta th13 (13 floats, same for the warp) and write the
 // window group's weighted error components to partial9 (lane 0). trace, when non-null, is
 // the [W][H][37] block of this theta.
+// LegWork fields that phase C reads, parked in shared memory between phase A and phase C so
+// that their registers are free during the reduction and the base solve. Of each velocity
+// product c_k = v_k x (S_k qd_k) only the four entries off the joint axis can be nonzero
+// (hip about x: w.y, w.z, v.y, v.z; thigh and calf about y: w.x, w.z, v.x, v.z); the zeros are
+// rebuilt on unparking. Field f of a thread lives at dst[f * stride].
+constexpr int kParkFloats = 42;
+__device__ __forceinline__ void park_legwork(const LegWork<float>& W, float* dst, int stride) {
+  int f = 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    dst[(f++) * stride] = W.U[k].w.x; dst[(f++) * stride] = W.U[k].w.y; dst[(f++) * stride] = W.U[k].w.z;
+    dst[(f++) * stride] = W.U[k].v.x; dst[(f++) * stride] = W.U[k].v.y; dst[(f++) * stride] = W.U[k].v.z;
+  }
+  dst[(f++) * stride] = W.cb[0].w.y; dst[(f++) * stride] = W.cb[0].w.z;
+  dst[(f++) * stride] = W.cb[0].v.y; dst[(f++) * stride] = W.cb[0].v.z;
+#pragma unroll
+  for (int k = 1; k < 3; ++k) {
+    dst[(f++) * stride] = W.cb[k].w.x; dst[(f++) * stride] = W.cb[k].w.z;
+    dst[(f++) * stride] = W.cb[k].v.x; dst[(f++) * stride] = W.cb[k].v.z;
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    dst[(f++) * stride] = W.invD[k]; dst[(f++) * stride] = W.u[k];
+    dst[(f++) * stride] = W.c[k]; dst[(f++) * stride] = W.s[k];
+  }
+}
+// Phase A's work record written straight to the parking area as each piece is produced
+// (same field layout as park_legwork), so that none of it occupies registers for the rest of
+// phase A.
+struct ParkedWork {
+  float* p;
+  int stride;
+  __device__ __forceinline__ void put_cs(int k, float c, float s) {
+    p[(30 + 4 * k + 2) * stride] = c;
+    p[(30 + 4 * k + 3) * stride] = s;
+  }
+  __device__ __forceinline__ void put_cb(int k, const SV<float>& v) {
+    if (k == 0) {
+      p[18 * stride] = v.w.y; p[19 * stride] = v.w.z; p[20 * stride] = v.v.y; p[21 * stride] = v.v.z;
+    } else {
+      const int f = 22 + 4 * (k - 1);
+      p[f * stride] = v.w.x; p[(f + 1) * stride] = v.w.z; p[(f + 2) * stride] = v.v.x; p[(f + 3) * stride] = v.v.z;
+    }
+  }
+  __device__ __forceinline__ void put_U(int k, const SV<float>& U, float invD, float u) {
+    float* q = p + 6 * k * stride;
+    q[0] = U.w.x; q[stride] = U.w.y; q[2 * stride] = U.w.z;
+    q[3 * stride] = U.v.x; q[4 * stride] = U.v.y; q[5 * stride] = U.v.z;
+    p[(30 + 4 * k) * stride] = invD;
+    p[(30 + 4 * k + 1) * stride] = u;
+  }
+};
+
+__device__ __forceinline__ void unpark_legwork(LegWork<float>& W, const float* src, int stride) {
+  int f = 0;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    W.U[k].w.x = src[(f++) * stride]; W.U[k].w.y = src[(f++) * stride]; W.U[k].w.z = src[(f++) * stride];
+    W.U[k].v.x = src[(f++) * stride]; W.U[k].v.y = src[(f++) * stride]; W.U[k].v.z = src[(f++) * stride];
+  }
+  W.cb[0].w.x = 0.f; W.cb[0].v.x = 0.f;
+  W.cb[0].w.y = src[(f++) * stride]; W.cb[0].w.z = src[(f++) * stride];
+  W.cb[0].v.y = src[(f++) * stride]; W.cb[0].v.z = src[(f++) * stride];
+#pragma unroll
+  for (int k = 1; k < 3; ++k) {
+    W.cb[k].w.y = 0.f; W.cb[k].v.y = 0.f;
+    W.cb[k].w.x = src[(f++) * stride]; W.cb[k].w.z = src[(f++) * stride];
+    W.cb[k].v.x = src[(f++) * stride]; W.cb[k].v.z = src[(f++) * stride];
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    W.invD[k] = src[(f++) * stride]; W.u[k] = src[(f++) * stride];
+    W.c[k] = src[(f++) * stride]; W.s[k] = src[(f++) * stride];
+  }
+}
+
 // One physics substep of a lane quad: phase A (leg), quad reduction, phase B (base solve),
-// phase C (leg). The 48-float LegWork of each lane is parked in shared memory between phase A
-// and phase C so that its registers are free during the reduction and the base solve;
-// [field][thread] layout keeps the accesses conflict-free. Blocks must be 128 threads. Every
-// kernel that steps the dynamics calls this one function.
+// phase C (leg), with the lane's LegWork parked in shared memory ([field][thread], conflict-
+// free) from phase A to phase C. Blocks must be 128 threads. Every kernel of
+// the quad layout that steps the dynamics calls this one function.
 __device__ __forceinline__ void substep(const DevModel& M, int leg, BaseState<float>& B, LegState<float>& L,
                                         const BaseParams<float>& bp, const LegParams<float>& lp,
                                         const float act[3]) {
-  __shared__ float lw_smem[(sizeof(LegWork<float>) / 4) * 128];
-  LegWork<float> lw;
-  LegOut<float> o = phase_a(M, leg, B, L, lp, act, lw);
-  {
-    const float* src = reinterpret_cast<const float*>(&lw);
-#pragma unroll
-    for (int f = 0; f < (int)(sizeof(LegWork<float>) / 4); ++f) lw_smem[f * 128 + threadIdx.x] = src[f];
-  }
+  __shared__ float lw_smem[kParkFloats * 128];
+  ParkedWork pw{lw_smem + threadIdx.x, 128};
+  LegOut<float> o = phase_a(M, leg, B, L, lp, act, pw);
   qsum_out(o);
   SV<float> a0 = phase_b(M, bp, o, B);
   LegWork<float> lw2;
-  {
-    float* dst = reinterpret_cast<float*>(&lw2);
-#pragma unroll
-    for (int f = 0; f < (int)(sizeof(LegWork<float>) / 4); ++f) dst[f] = lw_smem[f * 128 + threadIdx.x];
-  }
+  unpark_legwork(lw2, lw_smem + threadIdx.x, 128);
   phase_c(M, leg, a0, lw2, L);
 }
 

@@ -37,6 +37,7 @@ ENGINE_API = {
     "spi_set_cost": (c_int, [c_void_p, c_int, POINTER(c_float)]),
     "spi_run": (c_int, [c_void_p]),
     "spi_set_kernel_config": (c_int, [c_void_p, c_int]),
+    "spi_set_kernel_layout": (c_int, [c_void_p, c_int]),
     "spi_run_trace": (c_int, [c_void_p, c_void_p]),
     "spi_read_costs": (c_int, [c_void_p, c_void_p, c_void_p]),
     "spi_sync": (c_int, [c_void_p, POINTER(c_int64)]),

@@ -1,10 +1,13 @@
 """Kernel-variant autotuner for the rollout kernel.
 
-The rollout kernel comes in occupancy variants: the register allocator targets 3, 4 or 5
-CTAs of 128 threads per SM (168 / 128 / 96 registers per thread, with more spilling as
-registers shrink). Which is fastest depends on the horizon, window tiling and GPU, so the
-variant is picked by timing each on the caller's own windows and theta batch. Choices are
-cached per (GPU, horizon bucket, work bucket) in the build folder.
+The rollout kernel comes in two lane layouts -- "quad" (four lanes per rollout, one leg
+each) and "lane" (one lane per rollout through all four legs) -- and occupancy variants: the
+register allocator targets 2..5 CTAs of 128 threads per SM (255 / 168 / 128 / 96 registers
+per thread, with more spilling as registers shrink). Which is fastest depends on the
+horizon, the window count (the lane layout fills warps in blocks of 32 windows, the quad
+layout in groups of 8) and the GPU, so the variant is picked by timing each on the caller's
+own windows and theta batch. Choices are cached per (GPU, horizon bucket, work bucket,
+window-count remainder) in the build folder.
 """
 from __future__ import annotations
 
@@ -18,13 +21,16 @@ from . import _lib
 from ._build import LIB_DIR
 
 CACHE = LIB_DIR / "autotune.json"
-VARIANTS = (3, 4, 5)
+# (name, layout, min_blocks); layout 0 = SPI_LAYOUT_QUAD, 1 = SPI_LAYOUT_LANE
+VARIANTS = (("quad3", 0, 3), ("quad4", 0, 4), ("quad5", 0, 5), ("lane2", 1, 2), ("lane3", 1, 3))
+_BY_NAME = {v[0]: v for v in VARIANTS}
 
 
 def _key(engine):
     name = torch.cuda.get_device_name(engine.device).replace(" ", "_")
     work = engine.N * ((engine.W + 7) // 8)
-    return f"{name}|H{2 ** max(0, math.ceil(math.log2(max(engine.H, 1))))}|G{2 ** max(0, math.ceil(math.log2(max(work, 1))))}"
+    return (f"{name}|H{2 ** max(0, math.ceil(math.log2(max(engine.H, 1))))}"
+            f"|G{2 ** max(0, math.ceil(math.log2(max(work, 1))))}|W%32={engine.W % 32}")
 
 
 def _load():
@@ -34,9 +40,12 @@ def _load():
         return {}
 
 
-def set_variant(engine, min_blocks):
+def set_variant(engine, name):
+    """Select a rollout-kernel variant by name (one of VARIANTS)."""
+    _, layout, min_blocks = _BY_NAME[name]
+    _lib.check(engine.lib.spi_set_kernel_layout(engine._h, int(layout)))
     _lib.check(engine.lib.spi_set_kernel_config(engine._h, int(min_blocks)))
-    engine.min_blocks = int(min_blocks)
+    engine.variant = name
 
 
 def tune_engine(engine, reps=3, use_cache=True):
@@ -46,12 +55,12 @@ def tune_engine(engine, reps=3, use_cache=True):
     """
     cache = _load() if use_cache else {}
     key = _key(engine)
-    if use_cache and key in cache:
+    if use_cache and key in cache and cache[key]["best"] in _BY_NAME:
         set_variant(engine, cache[key]["best"])
         return cache[key]["best"], cache[key]["ms"]
     times = {}
     s = engine.stream
-    for mb in VARIANTS:
+    for mb, _, _ in VARIANTS:
         set_variant(engine, mb)
         engine.run()
         t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
