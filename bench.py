@@ -255,7 +255,7 @@ def run_ours(args):
     from spi_gb300.cem import CEM
     from spi_gb300.data import synthetic_windows
     from spi_gb300.engine import Engine, probe_fp32_peak
-    from spi_gb300.flops import flops_per_rollout_step
+    from spi_gb300.flops import executed_flops_per_rollout_step, flops_per_rollout_step
 
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
@@ -352,6 +352,10 @@ def run_ours(args):
             "kernel": ("rollout_lane_kernel" if variant.startswith("lane") else "rollout_kernel") + " (+finalize_costs)",
             "kernel_ms": kmean,
             "flops_per_rollout_step": fl,
+            "flops_note": "algorithmic count: the oracle's equations (legs by the articulated-body algorithm), "
+                          "instrumented on the host; the kernel condenses each leg through its joint-space "
+                          "inertia and executes executed_flops_per_rollout_step for the same result",
+            "executed_flops_per_rollout_step": executed_flops_per_rollout_step(cfg),
             "peak_source": "measured FP32 FMA-loop probe on this GPU (no FP32 entry in MEASURED_PEAKS.json)"}
     if rank != 0:
         if dist:

@@ -5,25 +5,28 @@
 // emulation (T = double, or a flop-counting scalar) that runs the phases in sequence.
 //
 // Phases of a substep (leg l = 0..3, FL FR RL RR):
-//   A  per leg : motor torques, leg kinematics, foot + 2 base-corner contacts, ABA
-//               backward pass of the 3-body chain -> the leg's articulated inertia and
-//               bias force expressed at the base (LegOut, 27 values)
+//   A  per leg : motor torques, leg kinematics, foot + 2 base-corner contacts, and the leg
+//               condensed onto the base through its 3x3 joint-space inertia (composite
+//               inertias, joint force columns, L D L^T, bias pass) -> the leg's articulated
+//               inertia and bias force expressed at the base (LegOut, 27 values), the same
+//               quantities as the backward pass of Featherstone's ABA
 //   (sum of the four LegOut: warp shuffles on the device, a loop on the host)
 //   B  base    : base articulated inertia + bias, 6x6 Cholesky solve for the base
 //               acceleration, semi-implicit Euler step of the floating base
-//   C  per leg : ABA forward pass (joint accelerations) and joint integration
+//   C  per leg : joint accelerations from the base acceleration (3x3 triangular solve) and
+//               joint integration
 //
 // Equations (Featherstone spatial algebra, motion = (w; v), force = (n; f)):
 //   PD law  tau = kp_s*Kp*(action_scale*clip(a) + q0 - q) - kd_s*Kd*qd, clipped to
 //           +-ts*tau_lim*(1 - |qd|/qd_max)+ -- spigym/envs/legged_base_task/
 //           legged_robot_base.py:185-187, 542-560 (hip action x hip_scale: go2_omni.py:437)
 //   motor   per-type gain and a*tanh(tau/a) -- spigym/envs/sysid/active_sysid_openloop.py:365-400
-//   joint   friction -Fc*tanh(qd/w_f); armature added to the ABA joint inertia D
+//   joint   friction -Fc*tanh(qd/w_f); armature added to the joint-space inertia diagonal
 //   contact fn = max(0, k*pen - c*s*vz) if pen > 0, s = min(1, pen/ramp) (damping fades in over
 //           the first `ramp` of penetration, so the force is continuous at touchdown);
 //           ft = -min(ct, mu*fn/|vt|)*vt. Contact damping is linearly implicit: an active
 //           contact adds a point mass dt*max(c, ct)*s at the contact point to its body's
-//           articulated inertia (exact for linear damping, stable at any dt)
+//           inertia (exact for linear damping, stable at any dt)
 //   base    nu += dt*a;  q <- normalise(q + dt/2 q(x)w_b);  p += dt*R(q)*v_b
 #pragma once
 
@@ -152,21 +155,6 @@ template <int AX, class T> SPI_INL S3<T> rot_sym(T c, T s, const S3<T>& M) {
   }
   return r;
 }
-// R B R^T for general B.
-template <int AX, class T> SPI_INL M3<T> rot_gen(T c, T s, const M3<T>& B) {
-  // rows of R B, then columns of (R B) R^T
-  V3<T> r0 = row(B, 0), r1 = row(B, 1), r2 = row(B, 2);
-  V3<T> q0, q1, q2;
-  if (AX == 1) { q0 = c * r0 + s * r2; q1 = r1; q2 = (-s) * r0 + c * r2; }
-  else { q0 = r0; q1 = c * r1 - s * r2; q2 = s * r1 + c * r2; }
-  M3<T> o;
-  V3<T> t0 = rot<AX>(c, s, q0), t1 = rot<AX>(c, s, q1), t2 = rot<AX>(c, s, q2);
-  o.m[0][0] = t0.x; o.m[0][1] = t0.y; o.m[0][2] = t0.z;
-  o.m[1][0] = t1.x; o.m[1][1] = t1.y; o.m[1][2] = t1.z;
-  o.m[2][0] = t2.x; o.m[2][1] = t2.y; o.m[2][2] = t2.z;
-  return o;
-}
-
 // I * v for an articulated inertia.
 template <class T> SPI_INL SV<T> mul(const Art<T>& I, const SV<T>& m) {
   SV<T> r;
@@ -204,62 +192,33 @@ template <class T> SPI_INL void add_to(Art<T>& a, const Art<T>& b) {
   for (int i = 0; i < 3; ++i)
     for (int j = 0; j < 3; ++j) a.B.m[i][j] += b.B.m[i][j];
 }
-// X^T I X for the joint transform X = plucker(R^T, r): rotate by the active joint rotation,
-// then shift by the joint origin r (child origin in parent coordinates):
-//   A' = A1 + P + P^T - [r]C1[r],  B' = B1 + [r]C1,  C' = C1,  P = [r] B1^T.
-template <int AX, int RM = 7, class T> SPI_INL Art<T> art_to_parent(const Art<T>& I, T c, T s, V3<T> r) {
-  Art<T> o;
-  S3<T> A1 = rot_sym<AX>(c, s, I.A);
-  M3<T> B1 = rot_gen<AX>(c, s, I.B);
-  S3<T> C1 = rot_sym<AX>(c, s, I.C);
-  if (RM == 4) {   // r = (0, 0, z)
-    const T z = r.z, zz = r.z * r.z;
-    o.A.xx = A1.xx - T(2) * z * B1.m[0][1] + zz * C1.yy;
-    o.A.yy = A1.yy + T(2) * z * B1.m[1][0] + zz * C1.xx;
-    o.A.zz = A1.zz;
-    o.A.xy = A1.xy + z * (B1.m[0][0] - B1.m[1][1]) - zz * C1.xy;
-    o.A.xz = A1.xz - z * B1.m[2][1];
-    o.A.yz = A1.yz + z * B1.m[2][0];
-    o.B.m[0][0] = B1.m[0][0] - z * C1.xy; o.B.m[0][1] = B1.m[0][1] - z * C1.yy; o.B.m[0][2] = B1.m[0][2] - z * C1.yz;
-    o.B.m[1][0] = B1.m[1][0] + z * C1.xx; o.B.m[1][1] = B1.m[1][1] + z * C1.xy; o.B.m[1][2] = B1.m[1][2] + z * C1.xz;
-    o.B.m[2][0] = B1.m[2][0]; o.B.m[2][1] = B1.m[2][1]; o.B.m[2][2] = B1.m[2][2];
-    o.C = C1;
-    return o;
-  }
-  if (RM == 2) {   // r = (0, y, 0)
-    const T y = r.y, yy = r.y * r.y;
-    o.A.xx = A1.xx + T(2) * y * B1.m[0][2] + yy * C1.zz;
-    o.A.yy = A1.yy;
-    o.A.zz = A1.zz - T(2) * y * B1.m[2][0] + yy * C1.xx;
-    o.A.xy = A1.xy + y * B1.m[1][2];
-    o.A.xz = A1.xz + y * (B1.m[2][2] - B1.m[0][0]) - yy * C1.xz;
-    o.A.yz = A1.yz - y * B1.m[1][0];
-    o.B.m[0][0] = B1.m[0][0] + y * C1.xz; o.B.m[0][1] = B1.m[0][1] + y * C1.yz; o.B.m[0][2] = B1.m[0][2] + y * C1.zz;
-    o.B.m[1][0] = B1.m[1][0]; o.B.m[1][1] = B1.m[1][1]; o.B.m[1][2] = B1.m[1][2];
-    o.B.m[2][0] = B1.m[2][0] - y * C1.xx; o.B.m[2][1] = B1.m[2][1] - y * C1.xy; o.B.m[2][2] = B1.m[2][2] - y * C1.xz;
-    o.C = C1;
-    return o;
-  }
-  // P = skew(r) B1^T: column j = r x (row j of B1)
-  V3<T> p0 = cross(r, row(B1, 0)), p1 = cross(r, row(B1, 1)), p2 = cross(r, row(B1, 2));
-  // Q = skew(r) C1: column j = r x (column j of C1);  skew(r) C1 skew(r): column j = r x (C1 (r x e_j))
-  V3<T> cq0 = cross(r, col(C1, 0)), cq1 = cross(r, col(C1, 1)), cq2 = cross(r, col(C1, 2));
-  V3<T> e0 = v3(T(0), r.z, -r.y), e1 = v3(-r.z, T(0), r.x), e2 = v3(r.y, -r.x, T(0));  // r x e_j
-  V3<T> k0 = cross(r, mul(C1, e0)), k1 = cross(r, mul(C1, e1)), k2 = cross(r, mul(C1, e2));
-  // A' = A1 + P + P^T - skew(r) C1 skew(r)
-  o.A.xx = A1.xx + T(2) * p0.x - k0.x;
-  o.A.yy = A1.yy + T(2) * p1.y - k1.y;
-  o.A.zz = A1.zz + T(2) * p2.z - k2.z;
-  o.A.xy = A1.xy + p1.x + p0.y - k1.x;
-  o.A.xz = A1.xz + p2.x + p0.z - k2.x;
-  o.A.yz = A1.yz + p2.y + p1.z - k2.y;
-  // B' = B1 + skew(r) C1
-  o.B.m[0][0] = B1.m[0][0] + cq0.x; o.B.m[0][1] = B1.m[0][1] + cq1.x; o.B.m[0][2] = B1.m[0][2] + cq2.x;
-  o.B.m[1][0] = B1.m[1][0] + cq0.y; o.B.m[1][1] = B1.m[1][1] + cq1.y; o.B.m[1][2] = B1.m[1][2] + cq2.y;
-  o.B.m[2][0] = B1.m[2][0] + cq0.z; o.B.m[2][1] = B1.m[2][1] + cq1.z; o.B.m[2][2] = B1.m[2][2] + cq2.z;
-  o.C = C1;
-  return o;
+// Rigid-body inertia as mass, first moment h = m c and rotational inertia about the body
+// origin (10 numbers; sums of rigid bodies stay rigid, so composite inertias use it too).
+template <class T> struct RI { T m; V3<T> h; S3<T> I; };
+template <class T> SPI_INL void ri_add(RI<T>& a, const RI<T>& b) {
+  a.m = a.m + b.m;
+  a.h = a.h + b.h;
+  a.I.xx += b.I.xx; a.I.yy += b.I.yy; a.I.zz += b.I.zz; a.I.xy += b.I.xy; a.I.xz += b.I.xz; a.I.yz += b.I.yz;
 }
+// Adds a point mass mp at p.
+template <class T> SPI_INL void ri_add_point(RI<T>& a, T mp, V3<T> p) {
+  const V3<T> hp = mp * p;
+  a.m = a.m + mp;
+  a.h = a.h + hp;
+  a.I.xx += hp.y * p.y + hp.z * p.z; a.I.yy += hp.x * p.x + hp.z * p.z; a.I.zz += hp.x * p.x + hp.y * p.y;
+  a.I.xy -= hp.x * p.y; a.I.xz -= hp.x * p.z; a.I.yz -= hp.y * p.z;
+}
+template <class T> SPI_INL SV<T> ri_mul(const RI<T>& a, const SV<T>& v) { return rigid_mul(a.m, a.h, a.I, v); }
+// I S for the revolute joint axis AX of the body's own frame: (I e_AX; e_AX x h).
+template <int AX, class T> SPI_INL SV<T> ri_col(const RI<T>& a) {
+  SV<T> f;
+  f.w = col(a.I, AX);
+  f.v = AX == 0 ? v3(T(0), -a.h.z, a.h.y) : v3(a.h.z, T(0), -a.h.x);
+  return f;
+}
+// Articulated-inertia form [[I, [h]x], [[h]x^T, m 1]].
+template <class T> SPI_INL Art<T> ri_art(const RI<T>& a) { return rigid(a.m, a.h, a.I); }
+
 // Joint-origin sparsity. RM = 2: origin on the y axis (thigh joints), RM = 4: on the z axis
 // (calf joints), RM = 7: general (hip joints). The model builder checks the pattern.
 // r x u for an origin r with zero components skipped.
@@ -291,6 +250,43 @@ template <int AX, int RM = 7, class T> SPI_INL SV<T> motion_to_child(const SV<T>
   SV<T> o;
   o.w = rotT<AX>(c, s, m.w);
   o.v = rotT<AX>(c, s, sub_rcross<RM>(m.v, r, m.w));
+  return o;
+}
+
+// X^T I X for a rigid inertia: the child's inertia in parent coordinates, child frame rotated
+// by the active joint rotation R about AX and placed at r. With a = R h:
+//   h' = a + m r,  I' = R I R^T + 2 (a.r) 1 - a r^T - r a^T + m (|r|^2 1 - r r^T).
+template <int AX, int RM, class T> SPI_INL RI<T> ri_to_parent(const RI<T>& c, T cs, T sn, V3<T> r) {
+  RI<T> o;
+  o.m = c.m;
+  const S3<T> I1 = rot_sym<AX>(cs, sn, c.I);
+  const V3<T> a = rot<AX>(cs, sn, c.h);
+  if (RM == 4) {   // r = (0, 0, z)
+    const T z = r.z, mz = c.m * z;
+    const T t = z * (T(2) * a.z + mz);
+    o.h = v3(a.x, a.y, a.z + mz);
+    o.I.xx = I1.xx + t; o.I.yy = I1.yy + t; o.I.zz = I1.zz;
+    o.I.xy = I1.xy; o.I.xz = I1.xz - a.x * z; o.I.yz = I1.yz - a.y * z;
+    return o;
+  }
+  if (RM == 2) {   // r = (0, y, 0)
+    const T y = r.y, my = c.m * y;
+    const T t = y * (T(2) * a.y + my);
+    o.h = v3(a.x, a.y + my, a.z);
+    o.I.xx = I1.xx + t; o.I.yy = I1.yy; o.I.zz = I1.zz + t;
+    o.I.xy = I1.xy - a.x * y; o.I.xz = I1.xz; o.I.yz = I1.yz - a.z * y;
+    return o;
+  }
+  const V3<T> mr = c.m * r;
+  o.h = a + mr;
+  const T ax = a.x * r.x, ay = a.y * r.y, az = a.z * r.z;
+  const T qx = mr.x * r.x, qy = mr.y * r.y, qz = mr.z * r.z;
+  o.I.xx = I1.xx + T(2) * (ay + az) + (qy + qz);
+  o.I.yy = I1.yy + T(2) * (ax + az) + (qx + qz);
+  o.I.zz = I1.zz + T(2) * (ax + ay) + (qx + qy);
+  o.I.xy = I1.xy - (a.x * r.y + a.y * r.x) - mr.x * r.y;
+  o.I.xz = I1.xz - (a.x * r.z + a.z * r.x) - mr.x * r.z;
+  o.I.yz = I1.yz - (a.y * r.z + a.z * r.y) - mr.y * r.z;
   return o;
 }
 
@@ -330,14 +326,19 @@ template <class T> struct LegState { T q[3], qd[3]; };
 template <class T> struct BaseParams { T m; V3<T> h; S3<T> Io; };   // base rigid inertia (+ fixed links)
 template <class T> struct LegParams { T kps, fc, arm, ts; };        // leg group's motor terms
 template <class T> struct LegOut { Art<T> I; SV<T> p; };            // leg contribution at the base
-template <class T> struct LegWork {                                 // phase A -> phase C
-  SV<T> U[3], cb[3];
-  T invD[3], u[3], c[3], s[3];
+// Phase A -> phase C. The leg's joint-space inertia factors as M = L D L^T (L unit lower
+// triangular: l10, l20, l21), the coupling to the base as K = F L^-T (F = the joints' spatial
+// force columns in base coordinates), so that qdd = L^-T (y - K'^T a0) with K' = K D^-1 and
+// y = D^-1 L^-1 (tau - C).
+template <class T> struct LegWork {
+  SV<T> Kp[3];
+  T y[3];
+  T l10, l20, l21;
   // phase A hands its results over through these (a kernel may store them elsewhere, e.g.
-  // straight to shared memory, with a type that has the same three members)
-  SPI_INL void put_cs(int k, T cc, T ss) { c[k] = cc; s[k] = ss; }
-  SPI_INL void put_cb(int k, const SV<T>& v) { cb[k] = v; }
-  SPI_INL void put_U(int k, const SV<T>& Uk, T invDk, T uk) { U[k] = Uk; invD[k] = invDk; u[k] = uk; }
+  // straight to shared memory, with a type that has the same members)
+  SPI_INL void put_K(int k, const SV<T>& v) { Kp[k] = v; }
+  SPI_INL void put_y(T y0, T y1, T y2) { y[0] = y0; y[1] = y1; y[2] = y2; }
+  SPI_INL void put_L(T a, T b, T c) { l10 = a; l20 = b; l21 = c; }
 };
 
 template <class T> SPI_INL M3<T> quat_to_R(T x, T y, T z, T w) {
@@ -417,18 +418,13 @@ template <class T> SPI_INL T motor_torque(const DevModel& M, const LegParams<T>&
 template <class T> SPI_INL V3<T> leg_org(const DevModel& M, int k, int leg) {
   return v3(T(M.org[k][0][leg]), T(M.org[k][1][leg]), T(M.org[k][2][leg]));
 }
-template <class T> SPI_INL Art<T> leg_rigid(const DevModel& M, int k, int leg) {
-  S3<T> Io;
-  Io.xx = T(M.I[k][0][leg]); Io.yy = T(M.I[k][1][leg]); Io.zz = T(M.I[k][2][leg]);
-  Io.xy = T(M.I[k][3][leg]); Io.xz = T(M.I[k][4][leg]); Io.yz = T(M.I[k][5][leg]);
-  return rigid(T(M.m[k][leg]), v3(T(M.h[k][0][leg]), T(M.h[k][1][leg]), T(M.h[k][2][leg])), Io);
-}
-template <class T> SPI_INL SV<T> leg_bias(const DevModel& M, int k, int leg, const SV<T>& v) {
-  S3<T> Io;
-  Io.xx = T(M.I[k][0][leg]); Io.yy = T(M.I[k][1][leg]); Io.zz = T(M.I[k][2][leg]);
-  Io.xy = T(M.I[k][3][leg]); Io.xz = T(M.I[k][4][leg]); Io.yz = T(M.I[k][5][leg]);
-  V3<T> h = v3(T(M.h[k][0][leg]), T(M.h[k][1][leg]), T(M.h[k][2][leg]));
-  return crf(v, rigid_mul(T(M.m[k][leg]), h, Io, v));
+template <class T> SPI_INL RI<T> leg_ri(const DevModel& M, int k, int leg) {
+  RI<T> r;
+  r.m = T(M.m[k][leg]);
+  r.h = v3(T(M.h[k][0][leg]), T(M.h[k][1][leg]), T(M.h[k][2][leg]));
+  r.I.xx = T(M.I[k][0][leg]); r.I.yy = T(M.I[k][1][leg]); r.I.zz = T(M.I[k][2][leg]);
+  r.I.xy = T(M.I[k][3][leg]); r.I.xz = T(M.I[k][4][leg]); r.I.yz = T(M.I[k][5][leg]);
+  return r;
 }
 
 // c = v x (S qd) for a revolute joint about axis AX.
@@ -438,39 +434,40 @@ template <int AX, class T> SPI_INL SV<T> vel_product(const SV<T>& v, T qd) {
   else { c.w = v3(-v.w.z * qd, T(0), v.w.x * qd); c.v = v3(-v.v.z * qd, T(0), v.v.x * qd); }
   return c;
 }
-
-// One ABA backward step of joint k (axis AX): project out the joint, move to the parent.
-template <int AX, int RM, class T, class WK>
-SPI_INL void aba_back(Art<T>& IA, SV<T>& pA, const SV<T>& cb, T tau, T arm, T c, T s, V3<T> r, WK& W, int k,
-                      Art<T>* Iout, SV<T>* pout) {
-  SV<T> U;
-  U.w = col(IA.A, AX);
-  U.v = row(IA.B, AX);
-  T D = (AX == 0 ? IA.A.xx : IA.A.yy) + arm;
-  T invD = T(1) / D;
-  T u = tau - (AX == 0 ? pA.w.x : pA.w.y);
-  // Ia = IA - U U^T / D
-  Art<T> Ia = IA;
-  V3<T> Uw = invD * U.w, Uv = invD * U.v;
-  Ia.A.xx -= Uw.x * U.w.x; Ia.A.yy -= Uw.y * U.w.y; Ia.A.zz -= Uw.z * U.w.z;
-  Ia.A.xy -= Uw.x * U.w.y; Ia.A.xz -= Uw.x * U.w.z; Ia.A.yz -= Uw.y * U.w.z;
-  Ia.B.m[0][0] -= Uw.x * U.v.x; Ia.B.m[0][1] -= Uw.x * U.v.y; Ia.B.m[0][2] -= Uw.x * U.v.z;
-  Ia.B.m[1][0] -= Uw.y * U.v.x; Ia.B.m[1][1] -= Uw.y * U.v.y; Ia.B.m[1][2] -= Uw.y * U.v.z;
-  Ia.B.m[2][0] -= Uw.z * U.v.x; Ia.B.m[2][1] -= Uw.z * U.v.y; Ia.B.m[2][2] -= Uw.z * U.v.z;
-  Ia.C.xx -= Uv.x * U.v.x; Ia.C.yy -= Uv.y * U.v.y; Ia.C.zz -= Uv.z * U.v.z;
-  Ia.C.xy -= Uv.x * U.v.y; Ia.C.xz -= Uv.x * U.v.z; Ia.C.yz -= Uv.y * U.v.z;
-  // pa = pA + Ia c + U u / D
-  SV<T> pa = mul(Ia, cb);
-  T uD = u * invD;
-  pa.w = pA.w + pa.w + uD * U.w;
-  pa.v = pA.v + pa.v + uD * U.v;
-  W.put_U(k, U, invD, u);
-  *Iout = art_to_parent<AX, RM>(Ia, c, s, r);
-  *pout = force_to_parent<AX, RM>(pa, c, s, r);
+template <class T> SPI_INL SV<T> operator+(const SV<T>& a, const SV<T>& b) {
+  SV<T> r; r.w = a.w + b.w; r.v = a.v + b.v; return r;
+}
+template <class T> SPI_INL SV<T> operator*(T s, const SV<T>& a) {
+  SV<T> r; r.w = s * a.w; r.v = s * a.v; return r;
+}
+// K - s J, componentwise.
+template <class T> SPI_INL SV<T> sub_scaled(const SV<T>& K, T s, const SV<T>& J) {
+  SV<T> r; r.w = K.w - s * J.w; r.v = K.v - s * J.v; return r;
+}
+// I -= a b^T for a symmetric rank-one a b^T (only the 21 stored entries).
+template <class T> SPI_INL void art_sub_outer(Art<T>& I, const SV<T>& a, const SV<T>& b) {
+  I.A.xx -= a.w.x * b.w.x; I.A.yy -= a.w.y * b.w.y; I.A.zz -= a.w.z * b.w.z;
+  I.A.xy -= a.w.x * b.w.y; I.A.xz -= a.w.x * b.w.z; I.A.yz -= a.w.y * b.w.z;
+  I.B.m[0][0] -= a.w.x * b.v.x; I.B.m[0][1] -= a.w.x * b.v.y; I.B.m[0][2] -= a.w.x * b.v.z;
+  I.B.m[1][0] -= a.w.y * b.v.x; I.B.m[1][1] -= a.w.y * b.v.y; I.B.m[1][2] -= a.w.y * b.v.z;
+  I.B.m[2][0] -= a.w.z * b.v.x; I.B.m[2][1] -= a.w.z * b.v.y; I.B.m[2][2] -= a.w.z * b.v.z;
+  I.C.xx -= a.v.x * b.v.x; I.C.yy -= a.v.y * b.v.y; I.C.zz -= a.v.z * b.v.z;
+  I.C.xy -= a.v.x * b.v.y; I.C.xz -= a.v.x * b.v.z; I.C.yz -= a.v.y * b.v.z;
 }
 
 // ---------------------------------------------------------------------------
 // Phase A: everything of one leg (and two base corners) up to its base contribution.
+//
+// The leg is condensed onto the base through its joint-space equations. With the base
+// acceleration a0 (gravity-shifted frame) as input, the leg obeys
+//   M qdd + F^T a0 + C = tau,    force on the base = I_c a0 + F qdd + p_c,
+// where I_c is the leg's composite rigid inertia at the base, F_k = I_k^c S_k the spatial force
+// column of joint k (composite inertia of the bodies below joint k times its axis), M the
+// 3x3 joint-space inertia plus armature, and (p_c, C) the bias force and joint bias torques of
+// a recursive Newton-Euler pass with a0 = 0, qdd = 0 (velocity products, the foot contact,
+// body velocity terms). Eliminating qdd gives the leg's articulated inertia and bias at the
+// base, I_c - F M^-1 F^T and p_c + F M^-1 (tau - C) -- the quantities Featherstone's ABA
+// backward pass produces, from fewer operations for a three-joint chain.
 // ---------------------------------------------------------------------------
 template <class T, class WK>
 SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
@@ -480,7 +477,6 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
   for (int k = 0; k < 3; ++k) {
     tau[k] = motor_torque(M, P, k, leg, act[k], L.q[k], L.qd[k]);
     m_sincos(L.q[k], &S[k], &C[k]);
-    W.put_cs(k, C[k], S[k]);
   }
   V3<T> r0 = leg_org<T>(M, 0, leg), r1 = leg_org<T>(M, 1, leg), r2 = leg_org<T>(M, 2, leg);
   // body velocities (body coordinates) and velocity-product accelerations
@@ -489,7 +485,6 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
   SV<T> v2 = motion_to_child<1, 4>(v1, C[2], S[2], r2);   v2.w.y = v2.w.y + L.qd[2];
   const SV<T> cb0 = vel_product<0>(v0, L.qd[0]), cb1 = vel_product<1>(v1, L.qd[1]),
               cb2 = vel_product<1>(v2, L.qd[2]);
-  W.put_cb(0, cb0); W.put_cb(1, cb1); W.put_cb(2, cb2);
   // foot: position and velocity, calf -> thigh -> hip -> base -> world
   V3<T> fc = v3(T(M.foot[0]), T(M.foot[1]), T(M.foot[2]));
   V3<T> vf = v2.v + cross(v2.w, fc);
@@ -501,28 +496,72 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
   vf = rot<0>(C[0], S[0], vf);
   T mimp;
   V3<T> F = contact_force(M, T(M.foot_r), B.p.z + dot(row(B.R, 2), pf), mul(B.R, vf), &mimp);
-  // the implicit point mass acts on the true acceleration while the ABA runs in the
+  // the implicit point mass acts on the true acceleration while the dynamics run in the
   // gravity-shifted frame: its share of the shift enters as a force mimp*g upwards
   F.z = F.z + mimp * T(M.g);
   V3<T> Fc = mulT(B.R, F);
   Fc = rotT<0>(C[0], S[0], Fc);
   Fc = rotT<1>(C[1], S[1], Fc);
   Fc = rotT<1>(C[2], S[2], Fc);
-  // ABA backward pass: calf -> thigh -> hip -> base
-  Art<T> IA = leg_rigid<T>(M, 2, leg);
-  add_point_mass(IA, mimp, fc);
-  SV<T> pA = leg_bias(M, 2, leg, v2);
-  pA.w = pA.w - cross(fc, Fc);
-  pA.v = pA.v - Fc;
-  Art<T> Ip; SV<T> pp;
-  aba_back<1, 4>(IA, pA, cb2, tau[2], P.arm, C[2], S[2], r2, W, 2, &Ip, &pp);
-  IA = leg_rigid<T>(M, 1, leg); add_to(IA, Ip);
-  pA = leg_bias(M, 1, leg, v1); pA.w = pA.w + pp.w; pA.v = pA.v + pp.v;
-  aba_back<1, 2>(IA, pA, cb1, tau[1], P.arm, C[1], S[1], r1, W, 1, &Ip, &pp);
-  IA = leg_rigid<T>(M, 0, leg); add_to(IA, Ip);
-  pA = leg_bias(M, 0, leg, v0); pA.w = pA.w + pp.w; pA.v = pA.v + pp.v;
+  // composite inertias: calf (+ the contact's implicit point mass at the foot) -> thigh -> hip
+  const RI<T> Ical = leg_ri<T>(M, 2, leg);
+  RI<T> Rc2 = Ical;
+  ri_add_point(Rc2, mimp, fc);
+  RI<T> Rc1 = leg_ri<T>(M, 1, leg);
+  ri_add(Rc1, ri_to_parent<1, 4>(Rc2, C[2], S[2], r2));
+  RI<T> Rc0 = leg_ri<T>(M, 0, leg);
+  ri_add(Rc0, ri_to_parent<1, 2>(Rc1, C[1], S[1], r1));
+  // bias pass (a0 = 0, qdd = 0): accelerations are the accumulated velocity products; the
+  // implicit point mass takes part in the inertial force, not in the velocity term
+  const SV<T> ab1 = motion_to_child<1, 2>(cb0, C[1], S[1], r1) + cb1;
+  const SV<T> ab2 = motion_to_child<1, 4>(ab1, C[2], S[2], r2) + cb2;
+  SV<T> f2 = crf(v2, ri_mul(Ical, v2)) + ri_mul(Rc2, ab2);
+  f2.w = f2.w - cross(fc, Fc);
+  f2.v = f2.v - Fc;
+  SV<T> f1;
+  {
+    const RI<T> Ith = leg_ri<T>(M, 1, leg);
+    f1 = force_to_parent<1, 4>(f2, C[2], S[2], r2) + (crf(v1, ri_mul(Ith, v1)) + ri_mul(Ith, ab1));
+  }
+  SV<T> f0;
+  {
+    const RI<T> Ihp = leg_ri<T>(M, 0, leg);
+    f0 = force_to_parent<1, 2>(f1, C[1], S[1], r1) + (crf(v0, ri_mul(Ihp, v0)) + ri_mul(Ihp, cb0));
+  }
+  const SV<T> pc = force_to_parent<0, 7>(f0, C[0], S[0], r0);
+  // joint force columns F_k = I_k^c S_k in base coordinates, and the joint-space inertia
+  const SV<T> F2t = force_to_parent<1, 4>(ri_col<1>(Rc2), C[2], S[2], r2);
+  const SV<T> F2h = force_to_parent<1, 2>(F2t, C[1], S[1], r1);
+  const SV<T> F1h = force_to_parent<1, 2>(ri_col<1>(Rc1), C[1], S[1], r1);
+  const SV<T> F0h = ri_col<0>(Rc0);
+  const T M00 = Rc0.I.xx + P.arm, M11 = Rc1.I.yy + P.arm, M22 = Rc2.I.yy + P.arm;
+  const T M01 = F1h.w.x, M02 = F2h.w.x, M12 = F2t.w.y;
+  // M = L D L^T
+  const T i0 = T(1) / M00;
+  const T l10 = M01 * i0, l20 = M02 * i0;
+  const T i1 = T(1) / (M11 - l10 * M01);
+  const T e12 = M12 - l20 * M01;
+  const T l21 = e12 * i1;
+  const T i2 = T(1) / (M22 - l20 * M02 - l21 * e12);
+  // K = F L^-T (base coordinates), K' = K D^-1, y = D^-1 L^-1 (tau - C)
+  const SV<T> K0 = force_to_parent<0, 7>(F0h, C[0], S[0], r0);
+  const SV<T> K1 = sub_scaled(force_to_parent<0, 7>(F1h, C[0], S[0], r0), l10, K0);
+  const SV<T> K2 = sub_scaled(sub_scaled(force_to_parent<0, 7>(F2h, C[0], S[0], r0), l20, K0), l21, K1);
+  const SV<T> Kp0 = i0 * K0, Kp1 = i1 * K1, Kp2 = i2 * K2;
+  const T z0 = tau[0] - f0.w.x;
+  const T z1 = (tau[1] - f1.w.y) - l10 * z0;
+  const T z2 = (tau[2] - f2.w.y) - l20 * z0 - l21 * z1;
+  const T y0 = z0 * i0, y1 = z1 * i1, y2 = z2 * i2;
+  W.put_K(0, Kp0); W.put_K(1, Kp1); W.put_K(2, Kp2);
+  W.put_y(y0, y1, y2);
+  W.put_L(l10, l20, l21);
+  // the leg at the base: articulated inertia I_c - K D^-1 K^T, bias p_c + K y
   LegOut<T> out;
-  aba_back<0, 7>(IA, pA, cb0, tau[0], P.arm, C[0], S[0], r0, W, 0, &out.I, &out.p);
+  out.I = ri_art(ri_to_parent<0, 7>(Rc0, C[0], S[0], r0));
+  art_sub_outer(out.I, Kp0, K0);
+  art_sub_outer(out.I, Kp1, K1);
+  art_sub_outer(out.I, Kp2, K2);
+  out.p = pc + (y0 * K0 + (y1 * K1 + y2 * K2));
   // two of the eight base-box corners; a corner can only reach the ground when the base origin
   // is lower than the box's half-diagonal, so a warp whose rollouts are all higher skips them
   // (a corner off the ground adds exactly zero force and zero implicit mass)
@@ -617,22 +656,19 @@ SPI_INL SV<T> phase_b(const DevModel& M, const BaseParams<T>& bp, const LegOut<T
 }
 
 // ---------------------------------------------------------------------------
-// Phase C: forward pass of one leg from the base acceleration, then joint integration.
+// Phase C: joint accelerations of one leg from the base acceleration, then joint integration:
+// qdd = L^-T (y - K'^T a0).
 // ---------------------------------------------------------------------------
-template <class T>
-SPI_INL void phase_c(const DevModel& M, int leg, const SV<T>& a0, const LegWork<T>& W, LegState<T>& L) {
+template <class T, class WK>
+SPI_INL void phase_c(const DevModel& M, int leg, const SV<T>& a0, const WK& W, LegState<T>& L) {
+  (void)leg;
+  const T w0 = W.y[0] - (dot(W.Kp[0].w, a0.w) + dot(W.Kp[0].v, a0.v));
+  const T w1 = W.y[1] - (dot(W.Kp[1].w, a0.w) + dot(W.Kp[1].v, a0.v));
+  const T w2 = W.y[2] - (dot(W.Kp[2].w, a0.w) + dot(W.Kp[2].v, a0.v));
   T qdd[3];
-  SV<T> a = motion_to_child<0>(a0, W.c[0], W.s[0], leg_org<T>(M, 0, leg));
-  a.w = a.w + W.cb[0].w; a.v = a.v + W.cb[0].v;
-  qdd[0] = (W.u[0] - dot(W.U[0].w, a.w) - dot(W.U[0].v, a.v)) * W.invD[0];
-  a.w.x = a.w.x + qdd[0];
-  a = motion_to_child<1, 2>(a, W.c[1], W.s[1], leg_org<T>(M, 1, leg));
-  a.w = a.w + W.cb[1].w; a.v = a.v + W.cb[1].v;
-  qdd[1] = (W.u[1] - dot(W.U[1].w, a.w) - dot(W.U[1].v, a.v)) * W.invD[1];
-  a.w.y = a.w.y + qdd[1];
-  a = motion_to_child<1, 4>(a, W.c[2], W.s[2], leg_org<T>(M, 2, leg));
-  a.w = a.w + W.cb[2].w; a.v = a.v + W.cb[2].v;
-  qdd[2] = (W.u[2] - dot(W.U[2].w, a.w) - dot(W.U[2].v, a.v)) * W.invD[2];
+  qdd[2] = w2;
+  qdd[1] = w1 - W.l21 * qdd[2];
+  qdd[0] = w0 - W.l10 * qdd[1] - W.l20 * qdd[2];
   T dt = T(M.dt);
 #pragma unroll
   for (int k = 0; k < 3; ++k) {

@@ -3,11 +3,14 @@
 // Runs phase A for the four legs, sums their contributions in the order the device quad
 // does ((leg0 + leg1) + (leg2 + leg3)), phase B once, phase C for the four legs. Used by
 // the tests to check the kernel's equations against the FP64 oracle on the CPU, and to
-// count the algorithmic FP operations of one substep (each operation once: the device
-// repeats phase B on the four lanes of a rollout, which is not counted).
+// count FP operations of one substep (each operation once: the device repeats phase B on
+// the four lanes of a rollout, which is not counted). The same driver runs the legs by
+// the articulated-body algorithm of the oracle (aba_reference.h): its count is the
+// algorithmic per-substep figure, and its results must equal the condensed phases'.
 #include <cmath>
 #include <cstring>
 
+#include "aba_reference.h"
 #include "model.h"
 
 namespace spi {
@@ -46,17 +49,24 @@ template <class T> static void add_out(LegOut<T>& a, const LegOut<T>& b) {
   a.p.v = a.p.v + b.p.v;
 }
 
-template <class T>
+// ABA = false: the kernel's condensed legs; true: the oracle's articulated-body algorithm.
+template <bool ABA, class T>
 static void substep(const DevModel& M, BaseState<T>& B, LegState<T> L[4], const BaseParams<T>& bp,
                     const LegParams<T> lp[4], const T act[12]) {
   LegWork<T> W[4];
+  aba::AbaWork<T> Wa[4];
   LegOut<T> o[4];
-  for (int leg = 0; leg < 4; ++leg) o[leg] = phase_a(M, leg, B, L[leg], lp[leg], act + 3 * leg, W[leg]);
+  for (int leg = 0; leg < 4; ++leg)
+    o[leg] = ABA ? aba::phase_a_aba(M, leg, B, L[leg], lp[leg], act + 3 * leg, Wa[leg])
+                 : phase_a(M, leg, B, L[leg], lp[leg], act + 3 * leg, W[leg]);
   add_out(o[0], o[1]);
   add_out(o[2], o[3]);
   add_out(o[0], o[2]);
   SV<T> a0 = phase_b(M, bp, o[0], B);
-  for (int leg = 0; leg < 4; ++leg) phase_c(M, leg, a0, W[leg], L[leg]);
+  for (int leg = 0; leg < 4; ++leg) {
+    if (ABA) aba::phase_c_aba(M, leg, a0, Wa[leg], L[leg]);
+    else phase_c(M, leg, a0, W[leg], L[leg]);
+  }
 }
 
 template <class T>
@@ -80,7 +90,7 @@ static void load_rollout(const DevModel& M, const double* x, const double* th, B
 
 using namespace spi;
 
-template <class T>
+template <bool ABA, class T>
 static int hostemu_rollout(const spi_robot* robot, const double* init, const double* actions,
                            const double* theta, int nb, int H, double* trace) {
   DevModel M;
@@ -97,7 +107,7 @@ static int hostemu_rollout(const spi_robot* robot, const double* init, const dou
       const double* a = actions + ((size_t)b * H + h) * 12;
       T act[12];
       for (int j = 0; j < 12; ++j) act[j] = T(a[j]);
-      for (int s = 0; s < M.decimation; ++s) substep(M, B, L, bp, lp, act);
+      for (int s = 0; s < M.decimation; ++s) substep<ABA>(M, B, L, bp, lp, act);
       double* out = trace + ((size_t)b * H + h) * SPI_STATE_DIM;
       T s13[13];
       base_to_world(B, s13);
@@ -112,23 +122,9 @@ static int hostemu_rollout(const spi_robot* robot, const double* init, const dou
   return SPI_OK;
 }
 
-extern "C" {
-
-// Rollouts through the kernel's phases on the host: init [B][37], actions [B][H][12],
-// theta [B][13] -> trace [B][H][37]; FP64, and FP32 (the device's arithmetic type).
-int spi_hostemu_rollout(const spi_robot* robot, const double* init, const double* actions,
-                        const double* theta, int nb, int H, double* trace) {
-  return hostemu_rollout<double>(robot, init, actions, theta, nb, H, trace);
-}
-int spi_hostemu_rollout_f32(const spi_robot* robot, const double* init, const double* actions,
-                            const double* theta, int nb, int H, double* trace) {
-  return hostemu_rollout<float>(robot, init, actions, theta, nb, H, trace);
-}
-
-// Algorithmic FP operations of one physics substep (whole rollout, phase B counted once)
-// and of the per-rollout setup (theta -> base inertia, world -> body velocity).
-int spi_hostemu_count_ops(const spi_robot* robot, const double* state, const double* theta,
-                          const double* act12, long long* per_substep, long long* per_rollout_setup) {
+template <bool ABA>
+static int count_ops(const spi_robot* robot, const double* state, const double* theta, const double* act12,
+                     long long* per_substep, long long* per_rollout_setup) {
   DevModel M;
   const char* why = "";
   int rc = build_dev_model(*robot, &M, &why);
@@ -143,9 +139,40 @@ int spi_hostemu_count_ops(const spi_robot* robot, const double* state, const dou
   Cf act[12];
   for (int j = 0; j < 12; ++j) act[j] = Cf(act12[j]);
   Cf::n = 0;
-  substep(M, B, L, bp, lp, act);
+  substep<ABA>(M, B, L, bp, lp, act);
   if (per_substep) *per_substep = Cf::n;
   return SPI_OK;
+}
+
+extern "C" {
+
+// Rollouts through the kernel's phases on the host: init [B][37], actions [B][H][12],
+// theta [B][13] -> trace [B][H][37]; FP64, and FP32 (the device's arithmetic type).
+int spi_hostemu_rollout(const spi_robot* robot, const double* init, const double* actions,
+                        const double* theta, int nb, int H, double* trace) {
+  return hostemu_rollout<false, double>(robot, init, actions, theta, nb, H, trace);
+}
+int spi_hostemu_rollout_f32(const spi_robot* robot, const double* init, const double* actions,
+                            const double* theta, int nb, int H, double* trace) {
+  return hostemu_rollout<false, float>(robot, init, actions, theta, nb, H, trace);
+}
+// The same rollouts with the legs by the articulated-body algorithm (FP64).
+int spi_hostemu_rollout_aba(const spi_robot* robot, const double* init, const double* actions,
+                            const double* theta, int nb, int H, double* trace) {
+  return hostemu_rollout<true, double>(robot, init, actions, theta, nb, H, trace);
+}
+
+// FP operations the kernel executes in one physics substep (whole rollout, phase B counted
+// once) and in the per-rollout setup (theta -> base inertia, world -> body velocity).
+int spi_hostemu_count_ops(const spi_robot* robot, const double* state, const double* theta,
+                          const double* act12, long long* per_substep, long long* per_rollout_setup) {
+  return count_ops<false>(robot, state, theta, act12, per_substep, per_rollout_setup);
+}
+// The same for the oracle's formulation (legs by the articulated-body algorithm): the
+// algorithmic count.
+int spi_hostemu_count_ops_aba(const spi_robot* robot, const double* state, const double* theta,
+                              const double* act12, long long* per_substep, long long* per_rollout_setup) {
+  return count_ops<true>(robot, state, theta, act12, per_substep, per_rollout_setup);
 }
 
 // Algorithmic FP operations of one substep per phase: [A (all four legs), B (base), C (all legs)].

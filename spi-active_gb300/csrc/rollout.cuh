@@ -64,80 +64,38 @@ __device__ __forceinline__ void load_model_smem(DevModel* dst, const DevModel* _
 // Roll one warp's eight windows for theta th13 (13 floats, same for the warp) and write the
 // window group's weighted error components to partial9 (lane 0). trace, when non-null, is
 // the [W][H][37] block of this theta.
-// LegWork fields that phase C reads, parked in shared memory between phase A and phase C so
-// that their registers are free during the reduction and the base solve. Of each velocity
-// product c_k = v_k x (S_k qd_k) only the four entries off the joint axis can be nonzero
-// (hip about x: w.y, w.z, v.y, v.z; thigh and calf about y: w.x, w.z, v.x, v.z); the zeros are
-// rebuilt on unparking. Field f of a thread lives at dst[f * stride].
-constexpr int kParkFloats = 42;
-__device__ __forceinline__ void park_legwork(const LegWork<float>& W, float* dst, int stride) {
-  int f = 0;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    dst[(f++) * stride] = W.U[k].w.x; dst[(f++) * stride] = W.U[k].w.y; dst[(f++) * stride] = W.U[k].w.z;
-    dst[(f++) * stride] = W.U[k].v.x; dst[(f++) * stride] = W.U[k].v.y; dst[(f++) * stride] = W.U[k].v.z;
-  }
-  dst[(f++) * stride] = W.cb[0].w.y; dst[(f++) * stride] = W.cb[0].w.z;
-  dst[(f++) * stride] = W.cb[0].v.y; dst[(f++) * stride] = W.cb[0].v.z;
-#pragma unroll
-  for (int k = 1; k < 3; ++k) {
-    dst[(f++) * stride] = W.cb[k].w.x; dst[(f++) * stride] = W.cb[k].w.z;
-    dst[(f++) * stride] = W.cb[k].v.x; dst[(f++) * stride] = W.cb[k].v.z;
-  }
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    dst[(f++) * stride] = W.invD[k]; dst[(f++) * stride] = W.u[k];
-    dst[(f++) * stride] = W.c[k]; dst[(f++) * stride] = W.s[k];
-  }
-}
-// Phase A's work record written straight to the parking area as each piece is produced
-// (same field layout as park_legwork), so that none of it occupies registers for the rest of
-// phase A.
+// The LegWork that phase C reads (24 floats: K'[3] 18, y 3, l10 / l20 / l21 3), parked in
+// shared memory between phase A and phase C so that its registers are free during the
+// reduction and the base solve. Field f of a thread lives at p[f * stride].
+constexpr int kParkFloats = 24;
+
+// Phase A's work record written straight to the parking area as each piece is produced, so
+// that none of it occupies registers for the rest of phase A.
 struct ParkedWork {
   float* p;
   int stride;
-  __device__ __forceinline__ void put_cs(int k, float c, float s) {
-    p[(30 + 4 * k + 2) * stride] = c;
-    p[(30 + 4 * k + 3) * stride] = s;
-  }
-  __device__ __forceinline__ void put_cb(int k, const SV<float>& v) {
-    if (k == 0) {
-      p[18 * stride] = v.w.y; p[19 * stride] = v.w.z; p[20 * stride] = v.v.y; p[21 * stride] = v.v.z;
-    } else {
-      const int f = 22 + 4 * (k - 1);
-      p[f * stride] = v.w.x; p[(f + 1) * stride] = v.w.z; p[(f + 2) * stride] = v.v.x; p[(f + 3) * stride] = v.v.z;
-    }
-  }
-  __device__ __forceinline__ void put_U(int k, const SV<float>& U, float invD, float u) {
+  __device__ __forceinline__ void put_K(int k, const SV<float>& v) {
     float* q = p + 6 * k * stride;
-    q[0] = U.w.x; q[stride] = U.w.y; q[2 * stride] = U.w.z;
-    q[3 * stride] = U.v.x; q[4 * stride] = U.v.y; q[5 * stride] = U.v.z;
-    p[(30 + 4 * k) * stride] = invD;
-    p[(30 + 4 * k + 1) * stride] = u;
+    q[0] = v.w.x; q[stride] = v.w.y; q[2 * stride] = v.w.z;
+    q[3 * stride] = v.v.x; q[4 * stride] = v.v.y; q[5 * stride] = v.v.z;
+  }
+  __device__ __forceinline__ void put_y(float y0, float y1, float y2) {
+    p[18 * stride] = y0; p[19 * stride] = y1; p[20 * stride] = y2;
+  }
+  __device__ __forceinline__ void put_L(float l10, float l20, float l21) {
+    p[21 * stride] = l10; p[22 * stride] = l20; p[23 * stride] = l21;
   }
 };
 
 __device__ __forceinline__ void unpark_legwork(LegWork<float>& W, const float* src, int stride) {
-  int f = 0;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    W.U[k].w.x = src[(f++) * stride]; W.U[k].w.y = src[(f++) * stride]; W.U[k].w.z = src[(f++) * stride];
-    W.U[k].v.x = src[(f++) * stride]; W.U[k].v.y = src[(f++) * stride]; W.U[k].v.z = src[(f++) * stride];
+    const float* q = src + 6 * k * stride;
+    W.Kp[k].w.x = q[0]; W.Kp[k].w.y = q[stride]; W.Kp[k].w.z = q[2 * stride];
+    W.Kp[k].v.x = q[3 * stride]; W.Kp[k].v.y = q[4 * stride]; W.Kp[k].v.z = q[5 * stride];
   }
-  W.cb[0].w.x = 0.f; W.cb[0].v.x = 0.f;
-  W.cb[0].w.y = src[(f++) * stride]; W.cb[0].w.z = src[(f++) * stride];
-  W.cb[0].v.y = src[(f++) * stride]; W.cb[0].v.z = src[(f++) * stride];
-#pragma unroll
-  for (int k = 1; k < 3; ++k) {
-    W.cb[k].w.y = 0.f; W.cb[k].v.y = 0.f;
-    W.cb[k].w.x = src[(f++) * stride]; W.cb[k].w.z = src[(f++) * stride];
-    W.cb[k].v.x = src[(f++) * stride]; W.cb[k].v.z = src[(f++) * stride];
-  }
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    W.invD[k] = src[(f++) * stride]; W.u[k] = src[(f++) * stride];
-    W.c[k] = src[(f++) * stride]; W.s[k] = src[(f++) * stride];
-  }
+  W.y[0] = src[18 * stride]; W.y[1] = src[19 * stride]; W.y[2] = src[20 * stride];
+  W.l10 = src[21 * stride]; W.l20 = src[22 * stride]; W.l21 = src[23 * stride];
 }
 
 // One physics substep of a lane quad: phase A (leg), quad reduction, phase B (base solve),

@@ -88,8 +88,12 @@ def hostemu_lib():
         lib.spi_hostemu_rollout.argtypes = [POINTER(SpiRobot), c_void_p, c_void_p, c_void_p, c_int, c_int, c_void_p]
         lib.spi_hostemu_rollout_f32.restype = c_int
         lib.spi_hostemu_rollout_f32.argtypes = lib.spi_hostemu_rollout.argtypes
+        lib.spi_hostemu_rollout_aba.restype = c_int
+        lib.spi_hostemu_rollout_aba.argtypes = lib.spi_hostemu_rollout.argtypes
         lib.spi_hostemu_count_ops.restype = c_int
         lib.spi_hostemu_count_ops.argtypes = [POINTER(SpiRobot), c_void_p, c_void_p, c_void_p,
                                               POINTER(ctypes.c_longlong), POINTER(ctypes.c_longlong)]
+        lib.spi_hostemu_count_ops_aba.restype = c_int
+        lib.spi_hostemu_count_ops_aba.argtypes = lib.spi_hostemu_count_ops.argtypes
         _hostemu = lib
     return _hostemu

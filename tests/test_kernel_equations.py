@@ -14,7 +14,11 @@ from oracle import spatial
 from oracle import sysid as osy
 from helpers import random_theta
 
-FLOPS_PER_SUBSTEP = 7053      # instrumented count of csrc/dynamics.cuh, default configuration, standing state (base-box corners off the ground)
+# Instrumented counts at the default configuration and a standing state (base-box corners off
+# the ground): the articulated-body formulation of the oracle (csrc/aba_reference.h), the
+# roofline's algorithmic figure, and the kernel's condensed formulation (csrc/dynamics.cuh).
+FLOPS_PER_SUBSTEP = 7053
+EXECUTED_FLOPS_PER_SUBSTEP = 5961
 
 
 def _emu(built, cfg, x0, acts, th):
@@ -101,6 +105,22 @@ def test_kernel_equations_reference_motor_variants(built, oracle_f32_constants):
         assert np.abs(emu - ref).max() < 1e-9, kw
 
 
+def test_condensed_legs_equal_articulated_body_algorithm(built):
+    """The kernel's leg condensation (joint-space inertia + Schur complement) and the oracle's
+    articulated-body algorithm, both in FP64 with the same constants, agree to rounding, in
+    and out of contact."""
+    from spi_gb300 import _lib, robot
+    cfg, x0, acts, th = _inputs(15, B=16, H=12)
+    x0[:8, 2] = 0.26                                   # half the rollouts start with feet pressed in
+    emu, r = _emu(built, cfg, x0, acts, th)
+    out = np.zeros_like(emu)
+    x0c, ac, tc = (np.ascontiguousarray(a, dtype=np.float64) for a in (x0, acts, th))
+    rc = _lib.hostemu_lib().spi_hostemu_rollout_aba(ctypes.byref(r), x0c.ctypes.data, ac.ctypes.data,
+                                                    tc.ctypes.data, x0.shape[0], acts.shape[1], out.ctypes.data)
+    assert rc == 0
+    assert np.abs(emu - out).max() < 1e-9
+
+
 def test_kernel_vs_oracle_with_urdf_constants(built):
     """Float32 model constants move states by < 1e-5 (well inside the 1e-4 parity bar)."""
     cfg, x0, acts, th = _inputs(13)
@@ -118,7 +138,15 @@ def test_flop_count_constant(built):
     x0c = np.ascontiguousarray(x0[0], dtype=np.float64)
     tc = np.ascontiguousarray(th[0], dtype=np.float64)
     ac = np.ascontiguousarray(acts[0, 0], dtype=np.float64)
-    rc = _lib.hostemu_lib().spi_hostemu_count_ops(ctypes.byref(r), x0c.ctypes.data, tc.ctypes.data,
-                                                  ac.ctypes.data, ctypes.byref(n1), ctypes.byref(n2))
+    lib = _lib.hostemu_lib()
+    rc = lib.spi_hostemu_count_ops_aba(ctypes.byref(r), x0c.ctypes.data, tc.ctypes.data,
+                                       ac.ctypes.data, ctypes.byref(n1), ctypes.byref(n2))
     assert rc == 0
     assert n1.value == FLOPS_PER_SUBSTEP
+    rc = lib.spi_hostemu_count_ops(ctypes.byref(r), x0c.ctypes.data, tc.ctypes.data,
+                                   ac.ctypes.data, ctypes.byref(n1), ctypes.byref(n2))
+    assert rc == 0
+    assert n1.value == EXECUTED_FLOPS_PER_SUBSTEP
+    from spi_gb300 import flops
+    assert flops.flops_per_rollout_step(cfg) == cfg.decimation * FLOPS_PER_SUBSTEP
+    assert flops.executed_flops_per_rollout_step(cfg) == cfg.decimation * EXECUTED_FLOPS_PER_SUBSTEP
