@@ -345,9 +345,9 @@ def run_ours(args):
     peak = probe_fp32_peak()
     achieved = steps_per_iter * fl / (kmean * 1e-3)
     roof = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": 422656,
+            "frac": achieved / peak, "traffic": 419328,
             "traffic_note": "dram read+write bytes per launch from ncu on 1024 theta x the same 256 windows "
-                            "(profiles/rollout_kernel_1024x256xH20_after_sparse.md); the window set is read once "
+                            "(profiles/rollout_kernel_1024x256xH20_full.md); the window set is read once "
                             "and theta / partials stay in L2, so traffic does not scale with theta",
             "kernel": ("rollout_lane_kernel" if variant.startswith("lane") else "rollout_kernel") + " (+finalize_costs)",
             "kernel_ms": kmean,
