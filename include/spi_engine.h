@@ -120,11 +120,15 @@ int spi_set_kernel_config(spi_engine* e, int min_blocks);
 
 /* Rollout-kernel lane layout. SPI_LAYOUT_QUAD: four lanes per rollout, one leg each, the base
  * solved on all four. SPI_LAYOUT_LANE: one lane per rollout through all four legs, the model
- * in the kernel's parameter block, 69 KB of shared memory per 128-thread CTA (so at most 3
+ * in the kernel's parameter block, 66 KB of shared memory per 128-thread CTA (so at most 3
  * CTAs per SM: min_blocks 2 or 3, larger values act as 3). Same equations, results within
  * FP32 rounding of each other; spi_run_trace always uses the quad layout. */
 #define SPI_LAYOUT_QUAD 0
 #define SPI_LAYOUT_LANE 1
+/* SPI_LAYOUT_BLOCK: the quad layout with each rollout's base solved once per substep by one
+ * warp of the CTA (one lane per rollout) instead of on all four of its lanes; two CTA
+ * barriers per substep; min_blocks 3..5. */
+#define SPI_LAYOUT_BLOCK 2
 int spi_set_kernel_layout(spi_engine* e, int layout);
 
 /* Roll every (theta, window) pair H control steps and reduce the windowed cost. Async. */

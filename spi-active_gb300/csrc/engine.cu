@@ -8,6 +8,7 @@
 #include "common.h"
 #include "model.h"
 #include "rollout.cuh"
+#include "rollout_block.cuh"
 #include "rollout_lane.cuh"
 #include "engine_impl.h"
 
@@ -76,6 +77,16 @@ int spi::run_impl(spi_engine* e, float* trace) {
     else
       rollout_lane_kernel<3><<<lgrid, 128, kLaneParkBytes, e->stream>>>(e->host_model, win, e->theta.f(), e->N, G,
                                                                         e->partial.f(), bad);
+  } else if (!trace && e->layout == SPI_LAYOUT_BLOCK) {
+    if (e->min_blocks == 4)
+      rollout_block_kernel<4><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
+                                                            e->partial.f(), bad);
+    else if (e->min_blocks == 5)
+      rollout_block_kernel<5><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
+                                                            e->partial.f(), bad);
+    else
+      rollout_block_kernel<3><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
+                                                            e->partial.f(), bad);
   } else if (trace)
     rollout_kernel<true, 3><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
                                                          e->partial.f(), trace, bad);
@@ -196,8 +207,8 @@ int spi_set_kernel_config(spi_engine* e, int min_blocks) {
 
 int spi_set_kernel_layout(spi_engine* e, int layout) {
   if (!e) return set_error(SPI_EINVAL, "null engine");
-  if (layout != SPI_LAYOUT_QUAD && layout != SPI_LAYOUT_LANE)
-    return set_error(SPI_EINVAL, "spi_set_kernel_layout: layout %d not 0/1", layout);
+  if (layout != SPI_LAYOUT_QUAD && layout != SPI_LAYOUT_LANE && layout != SPI_LAYOUT_BLOCK)
+    return set_error(SPI_EINVAL, "spi_set_kernel_layout: layout %d not 0/1/2", layout);
   if (layout == SPI_LAYOUT_LANE) {
     // the parking area is above the 48 KB default for dynamic shared memory
     cudaError_t ce = cudaFuncSetAttribute(rollout_lane_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,

@@ -5,12 +5,9 @@
 // eight). Per physics substep each lane runs phase A for legs FL, FR, RL, RR in turn, adding
 // their base contributions, solves the base once (phase B) and runs phase C for the four
 // legs. Compared with the quad layout (rollout.cuh) the base solve is not repeated on four
-// lanes, no shuffles combine the legs, and every model constant is read at a compile-time
-// offset of the kernel's parameter block (the model is passed by value), so the constants
-// are operands of the arithmetic instead of shared-memory loads.
+// lanes and no shuffles combine the legs; the model is passed by value in the kernel's
+// parameter block.
 //
-// The LegWork of legs FL, FR and RL is parked in shared memory ([leg][field][thread]) while
-// the later legs and the base solve run; RR's stays in registers.
 //
 // The error components of each window are formed at the final step, summed over each group
 // of eight lanes with xor-shuffles (the same tree as the quad layout's slot sum) and written
@@ -45,48 +42,60 @@ __device__ __forceinline__ float group8_sum(float x) {
   return x;
 }
 
-// Register budget: one lane holds four legs' joint states, the base state and the leg-sum
-// accumulators, so everything else lives in shared memory -- each leg's work record (written
-// by phase A as it is produced), the control step's actions, and the theta-derived base and
-// leg parameters (one copy per warp, all lanes share theta). The __syncwarp() between legs
-// keeps the compiler from interleaving the legs' arithmetic, which would need more registers
-// than the 168 that three CTAs per SM leave.
+// Code size and register budget: the four legs run in a loop that is not unrolled (four
+// unrolled copies of phase A overflow the instruction cache), so per-leg data is indexed at run
+// time: each leg's joint state, work record and actions live in shared memory, and the
+// model's per-leg constants are indexed loads from the kernel's parameter block. The
+// theta-derived base and leg parameters are one copy per warp (all lanes share theta).
 
-// Shared-memory layout per CTA: parking [3 legs][kParkFloats][128 threads], then actions
-// [12][128 threads].
-constexpr int kLaneParkBytes = (3 * kParkFloats + 12) * 128 * (int)sizeof(float);
+// Shared-memory layout per CTA, [field][128 threads] throughout: parking [4 legs][kParkFloats],
+// then joint states [4 legs][6] (q 3, qd 3), then actions [12].
+constexpr int kLaneLegState = 4 * kParkFloats * 128;
+constexpr int kLaneAct = kLaneLegState + 4 * 6 * 128;
+constexpr int kLaneParkBytes = (kLaneAct + 12 * 128) * (int)sizeof(float);
 
-// One physics substep of one rollout on one lane. park: this thread's first parking slot
-// (stride 128 floats between fields, kParkFloats * 128 between legs); act: this thread's first
-// action slot (stride 128); bp / lp: the warp's base and (front, rear) leg parameters.
-__device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>& B, LegState<float> (&L)[4],
-                                             const float* act, float* park, const BaseParams<float>* bp,
-                                             const LegParams<float>* lp) {
-  LegOut<float> sum;
-  LegWork<float> w3;
+__device__ __forceinline__ LegState<float> load_leg_state(const float* p) {
+  LegState<float> L;
 #pragma unroll
+  for (int k = 0; k < 3; ++k) { L.q[k] = p[k * 128]; L.qd[k] = p[(3 + k) * 128]; }
+  return L;
+}
+__device__ __forceinline__ void store_leg_state(const LegState<float>& L, float* p) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) { p[k * 128] = L.q[k]; p[(3 + k) * 128] = L.qd[k]; }
+}
+
+// One physics substep of one rollout on one lane. sm: this thread's first shared-memory slot
+// (fields 128 floats apart); bp / lp: the warp's base and (front, rear) leg parameters.
+__device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>& B, float* sm,
+                                             const BaseParams<float>* bp, const LegParams<float>* lp) {
+  LegOut<float> sum;
+  sum.I.A = S3<float>{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  sum.I.C = sum.I.A;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) sum.I.B.m[i][j] = 0.f;
+  sum.p.w = v3(0.f, 0.f, 0.f);
+  sum.p.v = sum.p.w;
+#pragma unroll 1
   for (int leg = 0; leg < 4; ++leg) {
-    const LegParams<float> P = lp[leg >= 2 ? 1 : 0];
-    const float a3[3] = {act[(3 * leg) * 128], act[(3 * leg + 1) * 128], act[(3 * leg + 2) * 128]};
-    if (leg < 3) {
-      ParkedWork pw{park + leg * kParkFloats * 128, 128};
-      LegOut<float> o = phase_a(M, leg, B, L[leg], P, a3, pw);
-      if (leg == 0) sum = o; else add_legout(sum, o);
-    } else {
-      LegOut<float> o = phase_a(M, leg, B, L[leg], P, a3, w3);
-      add_legout(sum, o);
-    }
-    __syncwarp();
+    const LegParams<float> P = lp[leg >> 1];
+    const float* ap = sm + kLaneAct + 3 * leg * 128;
+    const float a3[3] = {ap[0], ap[128], ap[256]};
+    const LegState<float> L = load_leg_state(sm + kLaneLegState + 6 * leg * 128);
+    ParkedWork pw{sm + leg * kParkFloats * 128, 128};
+    add_legout(sum, phase_a(M, leg, B, L, P, a3, pw));
   }
   const SV<float> a0 = phase_b(M, *bp, sum, B);
-  __syncwarp();
-  phase_c(M, 3, a0, w3, L[3]);
-#pragma unroll
-  for (int leg = 0; leg < 3; ++leg) {
-    __syncwarp();
+#pragma unroll 1
+  for (int leg = 0; leg < 4; ++leg) {
+    float* ls = sm + kLaneLegState + 6 * leg * 128;
+    LegState<float> L = load_leg_state(ls);
     LegWork<float> lw;
-    unpark_legwork(lw, park + leg * kParkFloats * 128, 128);
-    phase_c(M, leg, a0, lw, L[leg]);
+    unpark_legwork(lw, sm + leg * kParkFloats * 128, 128);
+    phase_c(M, leg, a0, lw, L);
+    store_leg_state(L, ls);
   }
 }
 
@@ -124,34 +133,39 @@ __global__ void __launch_bounds__(128, MINB) rollout_lane_kernel(const __grid_co
     __syncwarp();
   }
 
+  float* my_sm = lane_smem + threadIdx.x;
   BaseState<float> B;
-  LegState<float> L[4];
   {
     float s13[13];
 #pragma unroll
     for (int i = 0; i < 13; ++i) s13[i] = __ldg(win.init + i * W + w);
     base_from_world(B, s13);
 #pragma unroll
-    for (int leg = 0; leg < 4; ++leg)
+    for (int leg = 0; leg < 4; ++leg) {
+      LegState<float> L;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        L[leg].q[k] = __ldg(win.init + (13 + 3 * leg + k) * W + w);
-        L[leg].qd[k] = __ldg(win.init + (25 + 3 * leg + k) * W + w);
+        L.q[k] = __ldg(win.init + (13 + 3 * leg + k) * W + w);
+        L.qd[k] = __ldg(win.init + (25 + 3 * leg + k) * W + w);
       }
+      store_leg_state(L, my_sm + kLaneLegState + 6 * leg * 128);
+    }
   }
-  float* park = lane_smem + threadIdx.x;
-  float* act = lane_smem + 3 * kParkFloats * 128 + threadIdx.x;
   const int dec = M.decimation;
   for (int h = 0; h < H; ++h) {
     const float4* ap = reinterpret_cast<const float4*>(win.act + ((size_t)h * W + w) * 12);
+    float* act = my_sm + kLaneAct;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       const float4 a = __ldg(ap + i);
       act[(4 * i) * 128] = a.x; act[(4 * i + 1) * 128] = a.y;
       act[(4 * i + 2) * 128] = a.z; act[(4 * i + 3) * 128] = a.w;
     }
-    for (int s = 0; s < dec; ++s) substep_lane(M, B, L, act, park, &bp_warp[wib], lp_warp[wib]);
+    for (int s = 0; s < dec; ++s) substep_lane(M, B, my_sm, &bp_warp[wib], lp_warp[wib]);
   }
+  LegState<float> L[4];
+#pragma unroll
+  for (int leg = 0; leg < 4; ++leg) L[leg] = load_leg_state(my_sm + kLaneLegState + 6 * leg * 128);
   // final-step error components of this lane's window
   float s13[13];
   base_to_world(B, s13);

@@ -1,7 +1,8 @@
 """Kernel-variant autotuner for the rollout kernel.
 
-The rollout kernel comes in two lane layouts -- "quad" (four lanes per rollout, one leg
-each) and "lane" (one lane per rollout through all four legs) -- and occupancy variants: the
+The rollout kernel comes in three lane layouts -- "quad" (four lanes per rollout, one leg
+each), "block" (the quad layout with each rollout's base solved once by one warp of the CTA)
+and "lane" (one lane per rollout through all four legs) -- and occupancy variants: the
 register allocator targets 2..5 CTAs of 128 threads per SM (255 / 168 / 128 / 96 registers
 per thread, with more spilling as registers shrink). Which is fastest depends on the
 horizon, the window count (the lane layout fills warps in blocks of 32 windows, the quad
@@ -21,8 +22,9 @@ from . import _lib
 from ._build import LIB_DIR
 
 CACHE = LIB_DIR / "autotune.json"
-# (name, layout, min_blocks); layout 0 = SPI_LAYOUT_QUAD, 1 = SPI_LAYOUT_LANE
-VARIANTS = (("quad3", 0, 3), ("quad4", 0, 4), ("quad5", 0, 5), ("lane2", 1, 2), ("lane3", 1, 3))
+# (name, layout, min_blocks); layout 0 = SPI_LAYOUT_QUAD, 1 = SPI_LAYOUT_LANE, 2 = SPI_LAYOUT_BLOCK
+VARIANTS = (("quad3", 0, 3), ("quad4", 0, 4), ("quad5", 0, 5), ("lane2", 1, 2), ("lane3", 1, 3),
+            ("block3", 2, 3), ("block4", 2, 4), ("block5", 2, 5))
 _BY_NAME = {v[0]: v for v in VARIANTS}
 
 

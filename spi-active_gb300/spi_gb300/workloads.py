@@ -12,6 +12,7 @@ Both report aggregate rollout-steps/s and per-job latency (completion - arrival)
 from __future__ import annotations
 
 import time
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass
 
 import numpy as np
@@ -76,19 +77,28 @@ FISHER_CANDIDATES, FISHER_WINDOWS, FISHER_H = 32, 4, 20
 
 
 class FisherScorer:
-    """Excitation scoring at an identified theta (the Fisher request of a job)."""
+    """Excitation scoring at an identified theta (the Fisher request of a job).
 
-    def __init__(self, cfg: SimConfig | None = None, device=None):
+    With ``own_stream`` the scorer's engine and its torch work run on a private stream, so that
+    a worker thread can score while the caller keeps feeding the server."""
+
+    def __init__(self, cfg: SimConfig | None = None, device=None, own_stream=False):
         from .sensitivity import multisine_actions
-        self.engine = Engine(cfg, device=device)
+        self.stream = torch.cuda.Stream(device=device) if own_stream else None
+        self.engine = Engine(cfg, device=device, stream=self.stream)
         c = self.engine.cfg
         self.actions, _ = multisine_actions(FISHER_CANDIDATES, FISHER_WINDOWS * FISHER_H, c.control_dt,
                                             c.action_scale, seed=11, settle=100)
 
     def score(self, theta):
         from .sensitivity import score_excitations
-        r = score_excitations(self.engine, theta, self.actions, windows_per_cand=FISHER_WINDOWS, horizon=FISHER_H,
-                              settle=100)
+        if self.stream is not None:
+            with torch.cuda.stream(self.stream):
+                r = score_excitations(self.engine, theta, self.actions, windows_per_cand=FISHER_WINDOWS,
+                                      horizon=FISHER_H, settle=100)
+        else:
+            r = score_excitations(self.engine, theta, self.actions, windows_per_cand=FISHER_WINDOWS, horizon=FISHER_H,
+                                  settle=100)
         return {"best_candidate": r["best"], "logdet": float(r["logdet"][r["best"]])}
 
 
@@ -133,25 +143,36 @@ def default_work_cap(device=None):
 
 
 def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=64, hbm_budget=150 << 30,
-               ctas_per_sm=0, items_per_claim=1, realtime=True, work_cap=None):
+               ctas_per_sm=0, items_per_claim=1, realtime=True, work_cap=None, min_blocks=4):
     """Continuous batching: admit on arrival while HBM budget, a slot and GPU work capacity are free;
-    one CEM iteration per tick for every admitted job."""
+    one CEM iteration per tick for every admitted job. Fisher requests are scored on a worker
+    thread (own engine and stream) while the server keeps ticking; a job completes when its
+    score is in."""
     max_samples = max(s.n_samples for s in specs)
     server = Server(cfg, max_slots=max_slots, max_samples=max_samples, hbm_budget_bytes=hbm_budget,
                     device=bank.engine.device)
     server.config(ctas_per_sm, items_per_claim)
+    server.set_kernel_config(min_blocks)
     server.set_work_cap(default_work_cap(bank.engine.device) if work_cap is None else work_cap)
     jobs = {}
     for s in specs:                       # windows ready before the clock starts
         init, act, tgt = bank.get(s)
         jobs[s.job_id] = (Server.make_job(init, act, tgt, _cem_cfg(s), s.iterations), (init, act, tgt))
     pending = sorted(specs, key=lambda s: s.arrival)
-    scorer = FisherScorer(cfg, device=bank.engine.device) if any(s.fisher for s in specs) else None
+    scorer = FisherScorer(cfg, device=bank.engine.device, own_stream=True) if any(s.fisher for s in specs) else None
+    pool = ThreadPoolExecutor(max_workers=1) if scorer is not None else None
     by_id = {s.job_id: s for s in specs}
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    done, lat, results = 0, {}, {}
+    done, lat, results, scoring = 0, {}, {}, []
     qi = 0
+
+    def _score(job_id, theta, arrival):
+        with torch.cuda.device(bank.engine.device):
+            out = scorer.score(theta)
+        lat[job_id] = time.perf_counter() - t0 - arrival
+        return job_id, out
+
     while done < len(specs):
         now = time.perf_counter() - t0
         while qi < len(pending) and (pending[qi].arrival <= now or not realtime):
@@ -168,18 +189,27 @@ def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=
         for r in server.poll():
             spec = by_id[r["job_id"]]
             if spec.fisher:
-                r["fisher"] = scorer.score(r["best_theta"])
-            lat[r["job_id"]] = time.perf_counter() - t0 - spec.arrival
+                scoring.append(pool.submit(_score, r["job_id"], r["best_theta"], spec.arrival))
+            else:
+                lat[r["job_id"]] = time.perf_counter() - t0 - spec.arrival
             results[r["job_id"]] = r
             done += 1
+    for f in scoring:
+        job_id, out = f.result()
+        results[job_id]["fisher"] = out
     wall = time.perf_counter() - t0
+    if pool is not None:
+        pool.shutdown()
     server.close()
     return _summary(specs, lat, wall, results)
 
 
-def run_plain(specs, bank: WindowBank, cfg: SimConfig | None = None, graph=True):
-    """One job at a time through the single-job engine, in arrival order (FIFO)."""
+def run_plain(specs, bank: WindowBank, cfg: SimConfig | None = None, graph=True, variant="quad4"):
+    """One job at a time through the single-job engine, in arrival order (FIFO), with the
+    rollout-kernel variant the server runs (quad layout, 4 CTAs per SM by default)."""
+    from .autotune import set_variant
     eng = Engine(cfg, device=bank.engine.device)
+    set_variant(eng, variant)
     scorer = FisherScorer(cfg, device=bank.engine.device) if any(s.fisher for s in specs) else None
     order = sorted(specs, key=lambda s: s.arrival)
     for s in order:

@@ -1,9 +1,11 @@
-"""The lane-per-rollout layout of the rollout kernel (SPI_LAYOUT_LANE) against the FP64 oracle
-and against the quad layout.
+"""The rollout kernel's other layouts against the FP64 oracle and against the quad layout:
+SPI_LAYOUT_LANE (one lane per rollout through four legs) and SPI_LAYOUT_BLOCK (the quad
+layout with each rollout's base solved once per substep by one warp of the CTA).
 
 Tolerances as the quad layout's parity tests: window error components and costs <= 1e-4
-relative to the oracle cost scale; the two layouts agree within 1e-5 of the cost scale (they
-round differently: legs summed sequentially instead of by a shuffle tree).
+relative to the oracle cost scale; the layouts agree within 1e-5 of the cost scale (each is
+compiled separately, so multiply-add fusion, and the lane layout's leg summation order,
+differ).
 """
 import numpy as np
 import pytest
@@ -17,6 +19,7 @@ from helpers import oracle_windows, random_theta
 
 pytestmark = pytest.mark.gpu
 LANE_VARIANTS = ("lane2", "lane3")
+BLOCK_VARIANTS = ("block3", "block4", "block5")
 
 
 def _engine(init, actions, target, variant, weight=None, norm=None):
@@ -43,8 +46,8 @@ def _oracle_comp(init, actions, target, th):
     return oc.window_components(ref, np.tile(target.astype(np.float64), (N, 1))).reshape(N, W, 9).mean(1)
 
 
-@pytest.mark.parametrize("variant", LANE_VARIANTS)
-def test_lane_layout_matches_oracle_h20(built, variant):
+@pytest.mark.parametrize("variant", LANE_VARIANTS + BLOCK_VARIANTS)
+def test_layout_matches_oracle_h20(built, variant):
     """48 theta x 40 windows (one full and one partial block of 32) x H = 20."""
     rng = np.random.default_rng(200)
     _, init, actions, target = oracle_windows(11, n_traj=3, T=40, H=20)
@@ -59,38 +62,41 @@ def test_lane_layout_matches_oracle_h20(built, variant):
     assert cost_error(cost.cpu().numpy(), oc.scalar_cost(refc)) <= 1e-4
 
 
+@pytest.mark.parametrize("variant", ("lane3", "block4"))
 @pytest.mark.parametrize("W,H,N", [(1, 1, 1), (13, 3, 5), (33, 2, 9), (64, 5, 3)])
-def test_lane_layout_ragged_sizes(built, W, H, N):
+def test_layout_ragged_sizes(built, W, H, N, variant):
     rng = np.random.default_rng(W * 10 + H)
     _, init, actions, target = oracle_windows(W + 1, n_traj=1, T=W + H, H=H)
     init, actions, target = init[:W], actions[:W], target[:W]
     th = random_theta(rng, N).astype(np.float32)
-    e = _engine(init, actions, target, "lane3")
+    e = _engine(init, actions, target, variant)
     comp, _ = e.evaluate(torch.from_numpy(th))
     assert cost_error(comp.cpu().numpy(), _oracle_comp(init, actions, target, th)) <= 1e-4
 
 
-def test_lane_and_quad_layouts_agree(built):
+def test_layouts_agree(built):
     rng = np.random.default_rng(201)
     _, init, actions, target = oracle_windows(12, n_traj=4, T=60, H=10)
     init, actions, target = init[:100], actions[:100], target[:100]
     th = torch.from_numpy(random_theta(rng, 256).astype(np.float32))
     costs = {}
-    for v in ("quad3", "quad4", "lane2", "lane3"):
+    others = ("quad4", "quad5") + LANE_VARIANTS + BLOCK_VARIANTS
+    for v in ("quad3",) + others:
         e = _engine(init, actions, target, v)
         costs[v] = e.evaluate(th)[1].cpu().numpy()
-    for v in ("quad4", "lane2", "lane3"):
+    for v in others:
         assert cost_error(costs[v], costs["quad3"]) <= 1e-5, v
 
 
-def test_lane_layout_reference_cost_mode_and_mask(built):
+@pytest.mark.parametrize("variant", ("lane3", "block4"))
+def test_layout_reference_cost_mode_and_mask(built, variant):
     from oracle import windows as ow
     from spi_gb300.engine import COST_REF
     ds, init, actions, target = oracle_windows(2, n_traj=3, T=14, H=5, causal=False)
     mask = ow.eval_mask(ds["motion_ends"], 16)
     n_valid = ow.total_valid(ds["motion_ends"])
     th = random_theta(np.random.default_rng(3), 16).astype(np.float32)
-    e = _engine(init, actions, target, "lane3", weight=mask, norm=n_valid)
+    e = _engine(init, actions, target, variant, weight=mask, norm=n_valid)
     e.set_cost(COST_REF)
     comp, cost = e.evaluate(torch.from_numpy(th))
     refm = oc.reduce_components(osy.window_components(ds, th.astype(np.float64), gm.SimParams()), mask, n_valid)
@@ -98,12 +104,13 @@ def test_lane_layout_reference_cost_mode_and_mask(built):
     assert cost_error(cost.cpu().numpy(), oc.compute_cost(refm[:, :3])) <= 1e-4
 
 
-def test_lane_layout_deterministic_and_counts_nonfinite(built):
+@pytest.mark.parametrize("variant", ("lane3", "block4"))
+def test_layout_deterministic_and_counts_nonfinite(built, variant):
     rng = np.random.default_rng(8)
     _, init, actions, target = oracle_windows(3, n_traj=2, T=40, H=10)
     th = random_theta(rng, 40).astype(np.float32)
     th[5, 0] = np.nan
-    e = _engine(init, actions, target, "lane3")
+    e = _engine(init, actions, target, variant)
     c1 = e.evaluate(torch.from_numpy(th))[1].clone()
     bad = e.sync()
     c2 = e.evaluate(torch.from_numpy(th))[1].clone()
@@ -113,14 +120,14 @@ def test_lane_layout_deterministic_and_counts_nonfinite(built):
     assert np.isnan(c[5]) and np.isfinite(np.delete(c, 5)).all()
 
 
-def test_lane_layout_under_cem_graph(built):
-    """The CEM graph captures the lane kernel (model passed by value) and replays it."""
+def test_layouts_under_cem_graph(built):
+    """The CEM graph captures the lane kernel (model passed by value) and the block kernel."""
     from spi_gb300.autotune import set_variant
     from spi_gb300.cem import CEM
     from spi_gb300.engine import Engine
     _, init, actions, target = oracle_windows(4, n_traj=2, T=30, H=8)
     res = {}
-    for v in ("quad3", "lane3"):
+    for v in ("quad3", "lane3", "block4"):
         e = Engine()
         e.load_windows(torch.from_numpy(init), torch.from_numpy(actions), torch.from_numpy(target))
         set_variant(e, v)
@@ -129,5 +136,6 @@ def test_lane_layout_under_cem_graph(built):
         cem.run(3, graph=True)
         res[v] = cem.read()
     # the first iteration's population is identical; later ones may part at the ulp level
-    assert np.isfinite(res["lane3"]["best_cost"])
-    assert abs(np.log(res["lane3"]["best_cost"] / res["quad3"]["best_cost"])) < np.log(10.0)
+    for v in ("lane3", "block4"):
+        assert np.isfinite(res[v]["best_cost"])
+        assert abs(np.log(res[v]["best_cost"] / res["quad3"]["best_cost"])) < np.log(10.0)
