@@ -166,12 +166,13 @@ def _dist():
     return dist, dist.get_rank(), ws, local
 
 
-def served_vs_plain(specs, realtime, cfg=None):
-    """Run the same jobs served (continuous batching) and plain (one job at a time)."""
+def served_vs_plain(specs, realtime, cfg=None, variant="lane3"):
+    """Run the same jobs served (continuous batching) and plain (one job at a time), both on the
+    rollout-kernel variant `variant`."""
     from spi_gb300.workloads import WindowBank, run_plain, run_served
     bank = WindowBank(cfg)
-    served = run_served(specs, bank, cfg, realtime=realtime)
-    plain = run_plain(specs, bank, cfg)
+    served = run_served(specs, bank, cfg, realtime=realtime, variant=variant)
+    plain = run_plain(specs, bank, cfg, variant=variant)
     ratios = []
     for s in specs:
         a, b = served["results"][s.job_id]["best_cost"], plain["results"][s.job_id]["best_cost"]
@@ -184,8 +185,8 @@ def served_vs_plain(specs, realtime, cfg=None):
     # Correctness at the 1e-4 relative cost bar: one CEM iteration per job, served and plain. Both
     # paths score the same seeded prior population, so their best costs are comparable directly.
     one = [dataclasses.replace(s, iterations=1, arrival=0.0, fisher=False) for s in specs]
-    s1 = run_served(one, bank, cfg, realtime=False)["results"]
-    p1 = run_plain(one, bank, cfg)["results"]
+    s1 = run_served(one, bank, cfg, realtime=False, variant=variant)["results"]
+    p1 = run_plain(one, bank, cfg, variant=variant)["results"]
     errs = [abs(s1[s.job_id]["best_cost"] - p1[s.job_id]["best_cost"]) / max(abs(p1[s.job_id]["best_cost"]), 1e-30)
             for s in one]
     out["max_rel_cost_err_first_iteration"] = float(max(errs))
@@ -195,6 +196,7 @@ def served_vs_plain(specs, realtime, cfg=None):
     out["best_cost_ratio_served_over_plain"] = {"median": float(np.median(ratios)), "min": float(ratios.min()),
                                                 "max": float(ratios.max())}
     out["jobs"] = len(specs)
+    out["kernel_variant"] = variant
     return out
 
 
@@ -374,10 +376,13 @@ def run_ours(args):
             "cem": {"best_cost": cem.best_cost(), "theta_err": cem.theta_error(theta_true)}}
     if ws == 1 and not args.no_serving:
         from spi_gb300.workloads import c2_specs, small_specs
-        mix = served_vs_plain(c2_specs(args.mix_jobs, seed=2, iterations=args.mix_iters), False)
+        from spi_gb300.server import Server
+        sv = variant if variant in Server.VARIANTS else "lane3"
+        mix = served_vs_plain(c2_specs(args.mix_jobs, seed=2, iterations=args.mix_iters), False, variant=sv)
         mix["workload"] = (f"{args.mix_jobs} jobs of the c2 size distribution, {args.mix_iters} CEM iterations "
                            "each, all submitted at t=0")
-        small = served_vs_plain(small_specs(4 * args.mix_jobs, seed=3, iterations=args.mix_iters), False)
+        small = served_vs_plain(small_specs(4 * args.mix_jobs, seed=3, iterations=args.mix_iters), False,
+                                variant=sv)
         small["workload"] = (f"{4 * args.mix_jobs} small jobs (pop U{{64..512}}, W U{{8..64}}, H U{{5..20}}), "
                              f"{args.mix_iters} CEM iterations each, all submitted at t=0")
         line["served_vs_plain"] = {"c2_mix": mix, "small_jobs": small}

@@ -114,14 +114,15 @@ int spi_set_theta(spi_engine* e, const float* theta, int N);
 int spi_set_cost(spi_engine* e, int mode, const float* sq_weights);
 
 /* Rollout-kernel variant: the register allocator targets min_blocks CTAs of 128 threads per
- * SM (2: 255 registers; 3: 168; 4: 128; 5: 96; the quad layout takes 3..5, the lane layout
- * 2..3). Same equations; results within FP32 rounding of each other. */
+ * SM (2: 255 registers; 3: 168; 4: 128; 5: 96; the quad and block layouts take 3..5, the lane
+ * layout 2..4, larger values act as 4). Same equations; results within FP32 rounding of each
+ * other. */
 int spi_set_kernel_config(spi_engine* e, int min_blocks);
 
 /* Rollout-kernel lane layout. SPI_LAYOUT_QUAD: four lanes per rollout, one leg each, the base
  * solved on all four. SPI_LAYOUT_LANE: one lane per rollout through all four legs, the model
- * in the kernel's parameter block, 66 KB of shared memory per 128-thread CTA (so at most 3
- * CTAs per SM: min_blocks 2 or 3, larger values act as 3). Same equations, results within
+ * in the kernel's parameter block, 66 KB of shared memory per 128-thread CTA (min_blocks 2 or
+ * 3; min_blocks 4 keeps the last leg's work record in registers and needs 55 KB). Same equations, results within
  * FP32 rounding of each other; spi_run_trace always uses the quad layout. */
 #define SPI_LAYOUT_QUAD 0
 #define SPI_LAYOUT_LANE 1
@@ -262,8 +263,13 @@ int spi_server_stats(spi_server* s, int32_t* active, size_t* bytes_free);
 int spi_server_set_work_cap(spi_server* s, long long max_items);
 /* Persistent-grid shape: CTAs per SM (0 = occupancy maximum) and work items claimed per atomic. */
 int spi_server_config(spi_server* s, int ctas_per_sm, int items_per_claim);
-/* Rollout-kernel occupancy variant (3 or 4 CTAs of 128 threads per SM), as spi_set_kernel_config. */
+/* Rollout-kernel occupancy variant (CTAs of 128 threads per SM: 3 or 4 in the quad layout, 2 or
+ * 3 in the lane layout), as spi_set_kernel_config. */
 int spi_server_set_kernel_config(spi_server* s, int min_blocks);
+/* Rollout-kernel lane layout of the server: SPI_LAYOUT_QUAD (min_blocks 3 or 4) or
+ * SPI_LAYOUT_LANE (one lane per rollout, work items of 32 windows; min_blocks 2 or 3), as
+ * spi_set_kernel_layout. Only while no job is held (SPI_ESTATE otherwise). */
+int spi_server_set_kernel_layout(spi_server* s, int layout);
 
 /* ---- evaluation without any device allocation ---------------------------------------
  * No counterpart in the reference. For callers that must not let a library call cudaMalloc:

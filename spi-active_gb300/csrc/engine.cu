@@ -74,8 +74,11 @@ int spi::run_impl(spi_engine* e, float* trace) {
     if (e->min_blocks <= 2)
       rollout_lane_kernel<2><<<lgrid, 128, kLaneParkBytes, e->stream>>>(e->host_model, win, e->theta.f(), e->N, G,
                                                                         e->partial.f(), bad);
-    else
+    else if (e->min_blocks == 3)
       rollout_lane_kernel<3><<<lgrid, 128, kLaneParkBytes, e->stream>>>(e->host_model, win, e->theta.f(), e->N, G,
+                                                                        e->partial.f(), bad);
+    else
+      rollout_lane_kernel<4><<<lgrid, 128, kLanePeelBytes, e->stream>>>(e->host_model, win, e->theta.f(), e->N, G,
                                                                         e->partial.f(), bad);
   } else if (!trace && e->layout == SPI_LAYOUT_BLOCK) {
     if (e->min_blocks == 4)
@@ -216,6 +219,9 @@ int spi_set_kernel_layout(spi_engine* e, int layout) {
     if (ce == cudaSuccess)
       ce = cudaFuncSetAttribute(rollout_lane_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 kLaneParkBytes);
+    if (ce == cudaSuccess)
+      ce = cudaFuncSetAttribute(rollout_lane_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                kLanePeelBytes);
     if (ce != cudaSuccess) return cuda_error(ce, "spi_set_kernel_layout: shared-memory attribute");
   } else if (e->min_blocks < 3) {
     e->min_blocks = 3;

@@ -48,11 +48,15 @@ __device__ __forceinline__ float group8_sum(float x) {
 // model's per-leg constants are indexed loads from the kernel's parameter block. The
 // theta-derived base and leg parameters are one copy per warp (all lanes share theta).
 
-// Shared-memory layout per CTA, [field][128 threads] throughout: parking [4 legs][kParkFloats],
-// then joint states [4 legs][6] (q 3, qd 3), then actions [12].
-constexpr int kLaneLegState = 4 * kParkFloats * 128;
-constexpr int kLaneAct = kLaneLegState + 4 * 6 * 128;
-constexpr int kLaneParkBytes = (kLaneAct + 12 * 128) * (int)sizeof(float);
+// Shared-memory layout per CTA, [field][128 threads] throughout: parking [P legs][kParkFloats],
+// then joint states [4 legs][6] (q 3, qd 3), then actions [12]. P = 4, or 3 when the last leg's
+// work record stays in registers (PEEL, for the 4-CTA-per-SM variant, whose 128-register cap
+// leaves room for it and whose shared-memory share is 55 KB).
+template <bool PEEL> __host__ __device__ constexpr int lane_leg_state() { return (PEEL ? 3 : 4) * kParkFloats * 128; }
+template <bool PEEL> __host__ __device__ constexpr int lane_act() { return lane_leg_state<PEEL>() + 4 * 6 * 128; }
+template <bool PEEL> __host__ __device__ constexpr int lane_smem_bytes() { return (lane_act<PEEL>() + 12 * 128) * (int)sizeof(float); }
+constexpr int kLaneParkBytes = lane_smem_bytes<false>();
+constexpr int kLanePeelBytes = lane_smem_bytes<true>();
 
 __device__ __forceinline__ LegState<float> load_leg_state(const float* p) {
   LegState<float> L;
@@ -67,8 +71,10 @@ __device__ __forceinline__ void store_leg_state(const LegState<float>& L, float*
 
 // One physics substep of one rollout on one lane. sm: this thread's first shared-memory slot
 // (fields 128 floats apart); bp / lp: the warp's base and (front, rear) leg parameters.
+template <bool PEEL>
 __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>& B, float* sm,
                                              const BaseParams<float>* bp, const LegParams<float>* lp) {
+  constexpr int LS = lane_leg_state<PEEL>(), ACT = lane_act<PEEL>(), NP = PEEL ? 3 : 4;
   LegOut<float> sum;
   sum.I.A = S3<float>{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   sum.I.C = sum.I.A;
@@ -79,18 +85,31 @@ __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>
   sum.p.w = v3(0.f, 0.f, 0.f);
   sum.p.v = sum.p.w;
 #pragma unroll 1
-  for (int leg = 0; leg < 4; ++leg) {
+  for (int leg = 0; leg < NP; ++leg) {
     const LegParams<float> P = lp[leg >> 1];
-    const float* ap = sm + kLaneAct + 3 * leg * 128;
+    const float* ap = sm + ACT + 3 * leg * 128;
     const float a3[3] = {ap[0], ap[128], ap[256]};
-    const LegState<float> L = load_leg_state(sm + kLaneLegState + 6 * leg * 128);
+    const LegState<float> L = load_leg_state(sm + LS + 6 * leg * 128);
     ParkedWork pw{sm + leg * kParkFloats * 128, 128};
     add_legout(sum, phase_a(M, leg, B, L, P, a3, pw));
   }
+  LegWork<float> w3;
+  if (PEEL) {
+    const float* ap = sm + ACT + 9 * 128;
+    const float a3[3] = {ap[0], ap[128], ap[256]};
+    const LegState<float> L = load_leg_state(sm + LS + 18 * 128);
+    add_legout(sum, phase_a(M, 3, B, L, lp[1], a3, w3));
+  }
   const SV<float> a0 = phase_b(M, *bp, sum, B);
+  if (PEEL) {
+    float* ls = sm + LS + 18 * 128;
+    LegState<float> L = load_leg_state(ls);
+    phase_c(M, 3, a0, w3, L);
+    store_leg_state(L, ls);
+  }
 #pragma unroll 1
-  for (int leg = 0; leg < 4; ++leg) {
-    float* ls = sm + kLaneLegState + 6 * leg * 128;
+  for (int leg = 0; leg < NP; ++leg) {
+    float* ls = sm + LS + 6 * leg * 128;
     LegState<float> L = load_leg_state(ls);
     LegWork<float> lw;
     unpark_legwork(lw, sm + leg * kParkFloats * 128, 128);
@@ -99,30 +118,24 @@ __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>
   }
 }
 
-// One warp per (theta n, block of 32 windows); grid covers N * ceil(W / 32) warps; G is the
-// number of eight-window groups (ceil(W / 8)) of the partial layout. CTAs of 128 threads with
-// kLaneParkBytes of dynamic shared memory.
-template <int MINB>
-__global__ void __launch_bounds__(128, MINB) rollout_lane_kernel(const __grid_constant__ DevModel M, WinView win,
-                                                                 const float* __restrict__ theta, int N, int G,
-                                                                 float* __restrict__ partial,
-                                                                 unsigned long long* __restrict__ n_bad) {
-  extern __shared__ float lane_smem[];               // kLaneParkBytes
-  __shared__ BaseParams<float> bp_warp[4];
-  __shared__ LegParams<float> lp_warp[4][2];
-  const int WB = (win.W + 31) >> 5;
-  const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (warp >= (long long)N * WB) return;   // uniform per warp
-  const int n = (int)(warp / WB), wb = (int)(warp % WB);
+// One warp: theta th13 against windows [32 wb, 32 wb + 32) of win, writing the partials of the
+// four eight-window groups g = 4 wb .. 4 wb + 3 (those below G) to partial_n[g][SPI_N_COMP].
+// lane_smem: the CTA's lane_smem_bytes<PEEL>() of dynamic shared memory; bp_warp / lp_warp: the CTA's
+// per-warp parameter slots. Callable repeatedly by one warp (persistent kernels).
+template <bool PEEL>
+__device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinView& win, const float* th13, int wb,
+                                                  float* partial_n, int G, unsigned long long* n_bad,
+                                                  float* lane_smem, BaseParams<float>* bp_warp,
+                                                  LegParams<float> (*lp_warp)[2]) {
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int W = win.W, H = win.H;
   int w = wb * 32 + lane;
   const bool active = w < W;
   if (!active) w = W - 1;
 
+  __syncwarp();                      // the warp's previous item has finished with its slots
   {
     float th[SPI_THETA_DIM];
-    const float* th13 = theta + (size_t)n * SPI_THETA_DIM;
 #pragma unroll
     for (int i = 0; i < SPI_THETA_DIM; ++i) th[i] = __ldg(th13 + i);
     if (lane == 0) {
@@ -148,24 +161,24 @@ __global__ void __launch_bounds__(128, MINB) rollout_lane_kernel(const __grid_co
         L.q[k] = __ldg(win.init + (13 + 3 * leg + k) * W + w);
         L.qd[k] = __ldg(win.init + (25 + 3 * leg + k) * W + w);
       }
-      store_leg_state(L, my_sm + kLaneLegState + 6 * leg * 128);
+      store_leg_state(L, my_sm + lane_leg_state<PEEL>() + 6 * leg * 128);
     }
   }
   const int dec = M.decimation;
   for (int h = 0; h < H; ++h) {
     const float4* ap = reinterpret_cast<const float4*>(win.act + ((size_t)h * W + w) * 12);
-    float* act = my_sm + kLaneAct;
+    float* act = my_sm + lane_act<PEEL>();
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       const float4 a = __ldg(ap + i);
       act[(4 * i) * 128] = a.x; act[(4 * i + 1) * 128] = a.y;
       act[(4 * i + 2) * 128] = a.z; act[(4 * i + 3) * 128] = a.w;
     }
-    for (int s = 0; s < dec; ++s) substep_lane(M, B, my_sm, &bp_warp[wib], lp_warp[wib]);
+    for (int s = 0; s < dec; ++s) substep_lane<PEEL>(M, B, my_sm, &bp_warp[wib], lp_warp[wib]);
   }
   LegState<float> L[4];
 #pragma unroll
-  for (int leg = 0; leg < 4; ++leg) L[leg] = load_leg_state(my_sm + kLaneLegState + 6 * leg * 128);
+  for (int leg = 0; leg < 4; ++leg) L[leg] = load_leg_state(my_sm + lane_leg_state<PEEL>() + 6 * leg * 128);
   // final-step error components of this lane's window
   float s13[13];
   base_to_world(B, s13);
@@ -191,12 +204,31 @@ __global__ void __launch_bounds__(128, MINB) rollout_lane_kernel(const __grid_co
   const float wt = active ? __ldg(win.weight + w) : 0.f;
   const float comp[SPI_N_COMP] = {sqrtf(sp), sqrtf(sq), sqrtf(sj), sp, sq, sv, sw, sj, sjd};
   const int g = wb * 4 + (lane >> 3);
-  float* out = partial + ((size_t)n * G + g) * SPI_N_COMP;
+  float* out = partial_n + (size_t)g * SPI_N_COMP;
 #pragma unroll
   for (int k = 0; k < SPI_N_COMP; ++k) {
     const float v = group8_sum(active ? comp[k] * wt : 0.f);
     if ((lane & 7) == 0 && g < G) out[k] = v;
   }
+}
+
+// One warp per (theta n, block of 32 windows); grid covers N * ceil(W / 32) warps; G is the
+// number of eight-window groups (ceil(W / 8)) of the partial layout. CTAs of 128 threads with
+// lane_smem_bytes<(MINB >= 4)>() of dynamic shared memory.
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) rollout_lane_kernel(const __grid_constant__ DevModel M, WinView win,
+                                                                 const float* __restrict__ theta, int N, int G,
+                                                                 float* __restrict__ partial,
+                                                                 unsigned long long* __restrict__ n_bad) {
+  extern __shared__ float lane_smem[];               // lane_smem_bytes<(MINB >= 4)>()
+  __shared__ BaseParams<float> bp_warp[4];
+  __shared__ LegParams<float> lp_warp[4][2];
+  const int WB = (win.W + 31) >> 5;
+  const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (warp >= (long long)N * WB) return;   // uniform per warp
+  const int n = (int)(warp / WB), wb = (int)(warp % WB);
+  rollout_lane_warp<(MINB >= 4)>(M, win, theta + (size_t)n * SPI_THETA_DIM, wb, partial + (size_t)n * G * SPI_N_COMP,
+                                 G, n_bad, lane_smem, bp_warp, lp_warp);
 }
 
 }  // namespace spi

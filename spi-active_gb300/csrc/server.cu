@@ -18,6 +18,7 @@
 #include "common.h"
 #include "model.h"
 #include "rollout.cuh"
+#include "rollout_lane.cuh"
 
 using namespace spi;
 
@@ -109,6 +110,45 @@ __global__ void __launch_bounds__(128, MINB) server_rollout_kernel(const DevMode
   }
 }
 
+// The same in the lane layout: each work item is one (slot, theta, 32-window block), one lane
+// per window through all four legs (rollout_lane_warp). CTAs of 128 threads with kLaneParkBytes
+// of dynamic shared memory; the model by value.
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) server_rollout_lane_kernel(const __grid_constant__ DevModel M,
+                                                                  const SlotDesc* __restrict__ slots,
+                                                                  const int* __restrict__ order,
+                                                                  const TickInfo* __restrict__ info,
+                                                                  unsigned long long* __restrict__ counter,
+                                                                  unsigned long long* __restrict__ n_bad) {
+  extern __shared__ float lane_smem[];               // kLaneParkBytes
+  __shared__ BaseParams<float> bp_warp[4];
+  __shared__ LegParams<float> lp_warp[4][2];
+  const int lane = threadIdx.x & 31;
+  const long long total = info->total;
+  const int n_order = info->n_order, per = info->items_per_claim;
+  while (true) {
+    unsigned long long first = 0;
+    if (lane == 0) first = atomicAdd(counter, (unsigned long long)per);
+    first = __shfl_sync(0xffffffffu, first, 0);
+    if ((long long)first >= total) break;
+    for (int k = 0; k < per; ++k) {
+      const long long item = (long long)first + k;
+      if (item >= total) break;
+      int lo = 0, hi = n_order - 1;   // last slot whose range starts at or before item
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (slots[order[mid]].warp_begin <= item) lo = mid; else hi = mid - 1;
+      }
+      const SlotDesc& S = slots[order[lo]];
+      const long long local = item - S.warp_begin;
+      const int WB = (S.win.W + 31) >> 5;
+      const int n = (int)(local / WB), wb = (int)(local % WB);
+      rollout_lane_warp<false>(M, S.win, S.theta + (size_t)n * SPI_THETA_DIM, wb,
+                               S.partial + (size_t)n * S.G * SPI_N_COMP, S.G, n_bad, lane_smem, bp_warp, lp_warp);
+    }
+  }
+}
+
 __global__ void server_finalize_kernel(const SlotDesc* __restrict__ slots, int mode, float w0, float w1, float w2,
                                        float w3, float w4, float w5) {
   const SlotDesc& S = slots[blockIdx.y];
@@ -167,12 +207,26 @@ struct spi_server {
   int grid = 0, ctas_per_sm = 0, items_per_claim = 1;
   long long max_items = 0;         // admission cap on work items per tick (0: none)
   int min_blocks = 3;              // rollout kernel occupancy variant
+  int layout = SPI_LAYOUT_QUAD;    // SPI_LAYOUT_QUAD or SPI_LAYOUT_LANE
   int cost_mode = 1;
   float sq_w[6] = {10.f, 5.f, 0.1f, 0.1f, 1.f, 0.01f};
   long long ticks = 0;
 };
 
 namespace {
+
+// Work items of one slot per tick: (theta, 8-window group) in the quad layout, (theta, 32-window
+// block) in the lane layout.
+long long slot_items(const spi_server* s, const SlotDesc& d) {
+  const int per_theta = s->layout == SPI_LAYOUT_LANE ? (d.win.W + 31) / 32 : d.G;
+  return (long long)d.N * per_theta;
+}
+
+bool server_busy(const spi_server* s) {
+  for (const auto& sl : s->slots)
+    if (sl.used) return true;
+  return false;
+}
 
 void free_server(spi_server* s) {
   if (!s) return;
@@ -197,7 +251,14 @@ int enqueue_tick(spi_server* s) {
   cudaError_t ce = cudaMemsetAsync(s->d_counter, 0, sizeof(unsigned long long), s->stream);
   if (ce != cudaSuccess) return cuda_error(ce, "tick: reset counter");
   cem_sample_kernel<<<dim3(rows, s->max_slots), 128, 0, s->stream>>>(s->d_cem);
-  if (s->min_blocks == 4)
+  if (s->layout == SPI_LAYOUT_LANE) {
+    if (s->min_blocks <= 2)
+      server_rollout_lane_kernel<2><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
+          s->host_model, s->d_slots, s->d_order, s->d_info, s->d_counter, s->d_bad);
+    else
+      server_rollout_lane_kernel<3><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
+          s->host_model, s->d_slots, s->d_order, s->d_info, s->d_counter, s->d_bad);
+  } else if (s->min_blocks == 4)
     server_rollout_kernel<4><<<s->grid, 128, 0, s->stream>>>(s->d_model, s->d_slots, s->d_order, s->d_info,
                                                              s->d_counter, s->d_bad);
   else
@@ -235,9 +296,14 @@ int resize_grid(spi_server* s) {
   int dev = 0, sms = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaError_t ce = s->min_blocks == 4
-                       ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_kernel<4>, 128, 0)
-                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_kernel<3>, 128, 0);
+  cudaError_t ce;
+  if (s->layout == SPI_LAYOUT_LANE)
+    ce = s->min_blocks <= 2
+             ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_lane_kernel<2>, 128, kLaneParkBytes)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_lane_kernel<3>, 128, kLaneParkBytes);
+  else
+    ce = s->min_blocks == 4 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_kernel<4>, 128, 0)
+                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_kernel<3>, 128, 0);
   if (ce != cudaSuccess) return cuda_error(ce, "server: occupancy");
   const int per = s->ctas_per_sm > 0 ? std::min(s->ctas_per_sm, std::max(occ, 1)) : std::max(occ, 1);
   s->grid = sms * per;
@@ -342,9 +408,31 @@ int spi_server_config(spi_server* s, int ctas_per_sm, int items_per_claim) {
 
 int spi_server_set_kernel_config(spi_server* s, int min_blocks) {
   if (!s) return set_error(SPI_EINVAL, "null server");
-  if (min_blocks != 3 && min_blocks != 4)
-    return set_error(SPI_EINVAL, "spi_server_set_kernel_config: min_blocks %d not 3 or 4", min_blocks);
+  const int lo = s->layout == SPI_LAYOUT_LANE ? 2 : 3, hi = s->layout == SPI_LAYOUT_LANE ? 3 : 4;
+  if (min_blocks < lo || min_blocks > hi)
+    return set_error(SPI_EINVAL, "spi_server_set_kernel_config: min_blocks %d outside [%d, %d]", min_blocks, lo, hi);
   s->min_blocks = min_blocks;
+  return resize_grid(s);
+}
+
+int spi_server_set_kernel_layout(spi_server* s, int layout) {
+  if (!s) return set_error(SPI_EINVAL, "null server");
+  if (layout != SPI_LAYOUT_QUAD && layout != SPI_LAYOUT_LANE)
+    return set_error(SPI_EINVAL, "spi_server_set_kernel_layout: layout %d not 0/1", layout);
+  if (server_busy(s))
+    return set_error(SPI_ESTATE, "spi_server_set_kernel_layout: jobs in flight");
+  if (layout == SPI_LAYOUT_LANE) {
+    cudaError_t ce = cudaFuncSetAttribute(server_rollout_lane_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          kLaneParkBytes);
+    if (ce == cudaSuccess)
+      ce = cudaFuncSetAttribute(server_rollout_lane_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                kLaneParkBytes);
+    if (ce != cudaSuccess) return cuda_error(ce, "spi_server_set_kernel_layout: shared-memory attribute");
+    s->min_blocks = std::min(std::max(s->min_blocks, 2), 3);
+  } else {
+    s->min_blocks = std::min(std::max(s->min_blocks, 3), 4);
+  }
+  s->layout = layout;
   return resize_grid(s);
 }
 
@@ -369,8 +457,9 @@ int spi_server_submit(spi_server* s, const spi_job* job, int32_t* slot_out) {
   if (s->max_items > 0) {
     long long items = 0;
     for (const auto& o : s->slots)
-      if (o.active) items += (long long)o.desc.N * o.desc.G;
-    const long long mine = (long long)c.n_samples * ((job->W + 7) / 8);
+      if (o.active) items += slot_items(s, o.desc);
+    const long long mine =
+        (long long)c.n_samples * (s->layout == SPI_LAYOUT_LANE ? (job->W + 31) / 32 : (job->W + 7) / 8);
     if (items > 0 && items + mine > s->max_items)
       return set_error(SPI_EBUDGET, "spi_server_submit: GPU work cap reached (%lld + %lld items > %lld)", items,
                        mine, s->max_items);
@@ -493,7 +582,7 @@ int spi_server_tick(spi_server* s) {
   for (size_t k = 0; k < act.size(); ++k) {
     const int i = act[k];
     s->h_slots[i].warp_begin = begin;
-    begin += (long long)s->h_slots[i].N * s->h_slots[i].G;
+    begin += slot_items(s, s->h_slots[i]);
     s->h_order[k] = i;
   }
   s->h_info->total = begin;

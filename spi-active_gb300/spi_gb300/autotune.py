@@ -23,7 +23,7 @@ from ._build import LIB_DIR
 
 CACHE = LIB_DIR / "autotune.json"
 # (name, layout, min_blocks); layout 0 = SPI_LAYOUT_QUAD, 1 = SPI_LAYOUT_LANE, 2 = SPI_LAYOUT_BLOCK
-VARIANTS = (("quad3", 0, 3), ("quad4", 0, 4), ("quad5", 0, 5), ("lane2", 1, 2), ("lane3", 1, 3),
+VARIANTS = (("quad3", 0, 3), ("quad4", 0, 4), ("quad5", 0, 5), ("lane2", 1, 2), ("lane3", 1, 3), ("lane4", 1, 4),
             ("block3", 2, 3), ("block4", 2, 4), ("block5", 2, 5))
 _BY_NAME = {v[0]: v for v in VARIANTS}
 

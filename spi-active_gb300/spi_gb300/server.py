@@ -45,6 +45,7 @@ _API = {
     "spi_server_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "spi_server_wait": (ctypes.c_int, [ctypes.c_void_p]),
     "spi_server_set_kernel_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "spi_server_set_kernel_layout": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "spi_server_set_work_cap": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong]),
 }
 
@@ -146,6 +147,18 @@ class Server:
 
     def set_kernel_config(self, min_blocks):
         _lib.check(self.lib.spi_server_set_kernel_config(self._h, int(min_blocks)))
+
+    def set_kernel_layout(self, layout):
+        """0 = quad layout (4 lanes per rollout), 1 = lane layout (one lane per rollout)."""
+        _lib.check(self.lib.spi_server_set_kernel_layout(self._h, int(layout)))
+
+    # rollout-kernel variants the server runs, by the autotuner's names
+    VARIANTS = {"quad3": (0, 3), "quad4": (0, 4), "lane2": (1, 2), "lane3": (1, 3)}
+
+    def set_variant(self, name):
+        layout, min_blocks = self.VARIANTS[name]
+        self.set_kernel_layout(layout)
+        self.set_kernel_config(min_blocks)
 
     def set_work_cap(self, max_items):
         _lib.check(self.lib.spi_server_set_work_cap(self._h, int(max_items)))

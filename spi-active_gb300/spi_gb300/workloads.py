@@ -143,7 +143,7 @@ def default_work_cap(device=None):
 
 
 def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=64, hbm_budget=150 << 30,
-               ctas_per_sm=0, items_per_claim=1, realtime=True, work_cap=None, min_blocks=4):
+               ctas_per_sm=0, items_per_claim=1, realtime=True, work_cap=None, variant="lane3"):
     """Continuous batching: admit on arrival while HBM budget, a slot and GPU work capacity are free;
     one CEM iteration per tick for every admitted job. Fisher requests are scored on a worker
     thread (own engine and stream) while the server keeps ticking; a job completes when its
@@ -151,8 +151,8 @@ def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=
     max_samples = max(s.n_samples for s in specs)
     server = Server(cfg, max_slots=max_slots, max_samples=max_samples, hbm_budget_bytes=hbm_budget,
                     device=bank.engine.device)
+    server.set_variant(variant)
     server.config(ctas_per_sm, items_per_claim)
-    server.set_kernel_config(min_blocks)
     server.set_work_cap(default_work_cap(bank.engine.device) if work_cap is None else work_cap)
     jobs = {}
     for s in specs:                       # windows ready before the clock starts
@@ -204,9 +204,9 @@ def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=
     return _summary(specs, lat, wall, results)
 
 
-def run_plain(specs, bank: WindowBank, cfg: SimConfig | None = None, graph=True, variant="quad4"):
+def run_plain(specs, bank: WindowBank, cfg: SimConfig | None = None, graph=True, variant="lane3"):
     """One job at a time through the single-job engine, in arrival order (FIFO), with the
-    rollout-kernel variant the server runs (quad layout, 4 CTAs per SM by default)."""
+    rollout-kernel variant the server runs (lane layout, 3 CTAs per SM by default)."""
     from .autotune import set_variant
     eng = Engine(cfg, device=bank.engine.device)
     set_variant(eng, variant)

@@ -18,7 +18,7 @@ from oracle import sysid as osy
 from helpers import oracle_windows, random_theta
 
 pytestmark = pytest.mark.gpu
-LANE_VARIANTS = ("lane2", "lane3")
+LANE_VARIANTS = ("lane2", "lane3", "lane4")
 BLOCK_VARIANTS = ("block3", "block4", "block5")
 
 

@@ -24,19 +24,27 @@ def _run(server, jobs):
     return server.run_until_done(len(jobs))
 
 
-def test_same_result_alone_and_in_the_mix(built):
+def _server(variant="quad3", **kw):
     from spi_gb300.server import Server
+    s = Server(**kw)
+    s.set_variant(variant)
+    return s
+
+
+@pytest.mark.parametrize("variant", ["quad3", "lane3"])
+def test_same_result_alone_and_in_the_mix(built, variant):
     specs = [(1, 24, 5, 64, [0], 11), (2, 40, 9, 128, [0, 4, 5, 6], 12), (3, 16, 3, 96, list(range(13)), 13)]
-    mix = _run(Server(max_slots=8, max_samples=256), [_job(*s, iters=4) for s in specs])
+    mix = _run(_server(variant, max_slots=8, max_samples=256), [_job(*s, iters=4) for s in specs])
     for s in specs:
-        alone = _run(Server(max_slots=8, max_samples=256), [_job(*s, iters=4)])[s[-1]]
+        alone = _run(_server(variant, max_slots=8, max_samples=256), [_job(*s, iters=4)])[s[-1]]
         r = mix[s[-1]]
         assert r["iterations"] == 4
         assert np.array_equal(r["best_theta"], alone["best_theta"]) and r["best_cost"] == alone["best_cost"]
         assert np.array_equal(r["mu"], alone["mu"])
 
 
-def test_server_job_equals_engine_cem(built):
+@pytest.mark.parametrize("variant", ["quad3", "lane3"])
+def test_server_job_equals_engine_cem(built, variant):
     """A server job and the single-job engine CEM agree within the 1e-4 relative cost bar.
 
     The rollouts are the same code; the two cost-finalize kernels may contract the weighted
@@ -47,9 +55,11 @@ def test_server_job_equals_engine_cem(built):
     from spi_gb300.server import Server
     ids = [0, 1, 2, 4]
     job, (init, actions, target) = _job(4, 32, 6, 128, ids, 21, iters=5)
-    r = _run(Server(max_slots=4, max_samples=128), [(job, None)])[21]
+    r = _run(_server(variant, max_slots=4, max_samples=128), [(job, None)])[21]
+    from spi_gb300.autotune import set_variant
     e = Engine()
     e.load_windows(init, actions, target)
+    set_variant(e, variant)
     cem = CEM(e, n_samples=128, param_ids=ids, lo=gm.THETA_PRIOR_LO[ids], hi=gm.THETA_PRIOR_HI[ids],
               nominal=gm.THETA_NOMINAL, seed=104, job_id=21)
     for _ in range(5):
@@ -57,6 +67,17 @@ def test_server_job_equals_engine_cem(built):
     ref = cem.read()
     np.testing.assert_allclose(r["mu"], ref["mu"], rtol=1e-6)
     assert abs(ref["best_cost"] - r["best_cost"]) <= 1e-4 * abs(ref["best_cost"])
+
+
+def test_layout_switch_refused_while_jobs_are_held(built):
+    from spi_gb300 import _lib
+    s = _server("quad3", max_slots=2, max_samples=64)
+    job, keep = _job(8, 16, 4, 64, [0], 41)
+    assert s.submit(job) is not None
+    with pytest.raises(_lib.SpiError):
+        s.set_kernel_layout(1)
+    s.run_until_done(1)
+    s.set_kernel_layout(1)
 
 
 def test_admission_respects_budget_and_slots(built):
