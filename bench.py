@@ -347,11 +347,13 @@ def run_ours(args):
     peak = probe_fp32_peak()
     achieved = steps_per_iter * fl / (kmean * 1e-3)
     roof = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": 419328,
+            "frac": achieved / peak, "traffic": 419840 if variant.startswith("lane") else 419328,
             "traffic_note": "dram read+write bytes per launch from ncu on 1024 theta x the same 256 windows "
-                            "(profiles/rollout_kernel_1024x256xH20_full.md); the window set is read once "
-                            "and theta / partials stay in L2, so traffic does not scale with theta",
-            "kernel": ("rollout_lane_kernel" if variant.startswith("lane") else "rollout_kernel") + " (+finalize_costs)",
+                            "(profiles/rollout_lane_kernel_1024x256xH20.md, rollout_kernel_1024x256xH20_full.md); "
+                            "the window set is read once and theta / partials stay in L2, so traffic does not "
+                            "scale with theta",
+            "kernel": {"lane": "rollout_lane_kernel", "bloc": "rollout_block_kernel"}.get(variant[:4], "rollout_kernel")
+                      + " (+finalize_costs)",
             "kernel_ms": kmean,
             "flops_per_rollout_step": fl,
             "flops_note": "algorithmic count: the oracle's equations (legs by the articulated-body algorithm), "
