@@ -46,7 +46,8 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", choices=("c1", "c2", "c4"), default="c1")
+    ap.add_argument("--workload", choices=("c1", "c2", "c3", "c4"), default="c1")
+    ap.add_argument("--c3-candidates", type=int, default=512, help="c3: candidate excitations scored per step")
     ap.add_argument("--no-serving", action="store_true", help="c1: skip the served-vs-plain job mix")
     ap.add_argument("--mix-jobs", type=int, default=16, help="c1: jobs in the served-vs-plain mix")
     ap.add_argument("--mix-iters", type=int, default=10, help="c1: CEM iterations per job in the mix")
@@ -155,15 +156,9 @@ class ClockSampler:
 
 # --------------------------------------------------------------------------------------
 def _dist():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    if ws <= 1:
-        return None, 0, 1, 0
-    import torch
-    import torch.distributed as dist
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist.init_process_group("nccl")
-    return dist, dist.get_rank(), ws, local
+    from spi_gb300 import replicas
+    r = replicas.init("nccl" if int(os.environ.get("WORLD_SIZE", "1")) > 1 else None)
+    return r, r.rank, r.world, r.local
 
 
 def served_vs_plain(specs, realtime, cfg=None, variant="lane3"):
@@ -229,6 +224,62 @@ def run_multijob(args):
     print(json.dumps(line), flush=True)
 
 
+def run_c3(args):
+    """C3: score candidate excitations by the Fisher information of forward-mode state
+    sensitivities (13 theta directions x 37 states per window), BF16 J^T J on the tensor
+    cores, FP64 log det. One step = scoring all candidates once."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from spi_gb300.engine import Engine
+    from spi_gb300.robot import THETA_NOMINAL
+    from spi_gb300.sensitivity import block_weights, fisher, multisine_actions, score_excitations
+    torch.cuda.set_device(0)
+    eng = Engine()
+    cfg = eng.cfg
+    n, wpc, H, settle = args.c3_candidates, 8, 20, 100
+    acts, _ = multisine_actions(n, wpc * H, cfg.control_dt, cfg.action_scale, seed=3, settle=settle)
+    for _ in range(max(args.warmup, 1)):
+        r = score_excitations(eng, THETA_NOMINAL, acts, windows_per_cand=wpc, horizon=H, settle=settle)
+    torch.cuda.synchronize()
+    times = []
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            r = score_excitations(eng, THETA_NOMINAL, acts, windows_per_cand=wpc, horizon=H, settle=settle)
+            torch.cuda.synchronize()
+            times.append(time.perf_counter() - t0)
+    # the Fisher reduction alone, tensor cores against CUDA cores, on the last Jacobians
+    J, q = r["J"], block_weights((10.0, 5.0, 0.1, 0.1, 1.0, 0.01))
+    fisher_ms = {}
+    for name, tc in (("tensor_cores_bf16", True), ("cuda_cores_fp32", False)):
+        fisher(J, q, tensor_cores=tc)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(10):
+            fisher(J, q, tensor_cores=tc)
+        e1.record()
+        e1.synchronize()
+        fisher_ms[name] = e0.elapsed_time(e1) / 10
+    t = float(np.mean(times))
+    tangent_steps = n * wpc * H * 13
+    primal_steps = n * (settle + wpc * H)
+    line = {"metric": "excitation candidates scored/s", "value": n / t, "unit": "candidates/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": max(args.warmup, 1), "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (J), bf16 x bf16 -> f32 (J^T J), f64 (log det)",
+            "data": "synthetic",
+            "config": {"workload": f"c3: {n} multi-sine candidates (12 joints x 3 components, amplitude U(0.05, 0.4) "
+                                   f"rad, frequency U(0.5, 4) Hz), {settle}-step settle, {wpc} windows x H={H} "
+                                   f"per candidate, 13 x 37 forward-mode sensitivities per window",
+                       "step": "score every candidate once (settle trace, sensitivities, Fisher, log det)"},
+            "rollout_steps_per_s": (tangent_steps + primal_steps) / t,
+            "tangent_rollout_steps_per_step": tangent_steps, "primal_rollout_steps_per_step": primal_steps,
+            "fisher_ms": fisher_ms, "best_candidate": int(r["best"]),
+            "logdet_range": [float(np.min(r["logdet"])), float(np.max(r["logdet"]))],
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -247,12 +298,11 @@ def run_reference(args):
 
 def run_ours(args):
     import torch
-    dist, rank, ws, local = _dist()
     import __graft_entry__
-    if rank == 0:
+    if int(os.environ.get("RANK", "0")) == 0:
         __graft_entry__.build()
-    if dist:
-        dist.barrier()
+    ranks, rank, ws, local = _dist()
+    ranks.barrier()
     from spi_gb300 import robot
     from spi_gb300.cem import CEM
     from spi_gb300.data import synthetic_windows
@@ -286,8 +336,7 @@ def run_ours(args):
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     run_s = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     run_e = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    if dist:
-        dist.barrier()
+    ranks.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
         wall0 = time.perf_counter()
@@ -300,14 +349,9 @@ def run_ours(args):
         wall = time.perf_counter() - wall0
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     kern_ms = [s.elapsed_time(e) for s, e in zip(run_s, run_e)]
-    total_ms = float(np.sum(step_ms))
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
     n_bad = eng.sync()
     steps_per_iter = N * W * H
-    value = ws * steps_per_iter * args.steps / (total_ms * 1e-3)
+    value, total_ms = ranks.whole_job_rate(steps_per_iter * args.steps, float(np.sum(step_ms)), dev)
 
     # end to end: host buffers through the public API, copies inside the timed region
     e2e = None
@@ -335,9 +379,10 @@ def run_ours(args):
             h_cost.copy_(cost, non_blocking=True)
         e1.record(stream)
         torch.cuda.synchronize()
-        e2e_ms = e0.elapsed_time(e1)
+        ranks.barrier()
+        e2e_value, e2e_ms = ranks.whole_job_rate(steps_per_iter * args.steps, e0.elapsed_time(e1), dev)
         h2d = (init.nbytes + actions.nbytes + target.nbytes + N * 13 * 4)
-        e2e = {"value": ws * steps_per_iter * args.steps / (e2e_ms * 1e-3), "unit": METRIC,
+        e2e = {"value": e2e_value, "unit": METRIC,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(N * 4),
                "note": "per step: windows + theta H2D from pinned memory, spi_load_windows, "
                        "spi_set_theta, spi_run, spi_read_costs, cost D2H (evaluation only)"}
@@ -362,8 +407,7 @@ def run_ours(args):
             "executed_flops_per_rollout_step": executed_flops_per_rollout_step(cfg),
             "peak_source": "measured FP32 FMA-loop probe on this GPU (no FP32 entry in MEASURED_PEAKS.json)"}
     if rank != 0:
-        if dist:
-            dist.destroy_process_group()
+        ranks.close()
         return
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -391,14 +435,15 @@ def run_ours(args):
     if ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds, H)
     print(json.dumps(line), flush=True)
-    if dist:
-        dist.destroy_process_group()
+    ranks.close()
 
 
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "c3":
+        run_c3(args)
     elif args.workload in ("c2", "c4"):
         run_multijob(args)
     else:
