@@ -30,7 +30,14 @@ def _f32(t, shape, name, device):
 
 
 class Engine:
-    def __init__(self, cfg: SimConfig | None = None, device=None, stream: torch.cuda.Stream | None = None):
+    """Batched evaluation of theta samples against logged windows (the C ABI's spi_engine).
+
+    variant: the rollout-kernel variant (see spi_gb300.autotune.VARIANTS). The default, lane3
+    (one lane per rollout, 3 CTAs per SM), is the fastest on the C1 workload;
+    spi_gb300.autotune.tune_engine times every variant on the caller's own batch."""
+
+    def __init__(self, cfg: SimConfig | None = None, device=None, stream: torch.cuda.Stream | None = None,
+                 variant: str | None = "lane3"):
         if not torch.cuda.is_available():
             raise RuntimeError("spi_gb300.Engine needs a CUDA device (no CPU fallback exists)")
         self.cfg = cfg or SimConfig()
@@ -45,6 +52,10 @@ class Engine:
         _lib.check(self.lib.spi_set_stream(self._h, ctypes.c_void_p(self.stream.cuda_stream)))
         self.W = self.H = self.N = 0
         self._keep = []
+        if variant is not None:
+            from .autotune import set_variant
+            with torch.cuda.device(self.device):
+                set_variant(self, variant)
 
     def close(self):
         if getattr(self, "_h", None):
