@@ -281,18 +281,43 @@ def run_c3(args):
 
 
 def run_reference(args):
+    """The reference arm: the FP64 oracle (the reference path's CPU restatement) on all host
+    cores, W warm-up steps then K timed steps. One step is a bounded sample of the C1 workload:
+    one task per core of 8 theta x 32 windows x H = 20 rollouts."""
+    import multiprocessing as mp
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    base = cpu_baseline(args.cpu_seconds, C1["horizon"])
-    line = {"metric": METRIC, "value": base["value"], "unit": METRIC, "impl": "reference",
+    cores = os.cpu_count() or 1
+    H = C1["horizon"]
+    per_task = (8, 32, H)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        pool.map(_oracle_chunk, [(i, 1, 8, 2) for i in range(cores)])   # import warm-up
+        task = 0
+        for _ in range(args.warmup):
+            pool.map(_oracle_chunk, [(1000 + task + i, *per_task) for i in range(cores)])
+            task += cores
+        step_s, done = [], 0
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            res = pool.map(_oracle_chunk, [(1000 + task + i, *per_task) for i in range(cores)])
+            step_s.append(time.perf_counter() - t0)
+            task += cores
+            done += sum(r[0] for r in res)
+    total = float(np.sum(step_s))
+    value = done / total
+    sample = (f"{args.steps} steps x {cores} tasks x (8 theta x 32 windows x H={H}) of the c1 workload, "
+              f"{done} rollout-steps in {total:.1f} s (FP64 NumPy oracle, spawn pool, after {args.warmup} "
+              f"warm-up steps)")
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": C1["n_theta"] * C1["n_windows"] * C1["horizon"] / base["value"] * 1e3,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": "c1: 4096 theta x 256 windows x H=20, 13 params, "
-                                                        "Go2 FP64 NumPy oracle on host cores"},
-            "cpu_baseline": base,
-            "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "ms_per_step": total * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "c1: 4096 theta x 256 windows x H=20, 13 params, Go2 FP64 NumPy oracle on "
+                                   "host cores", "step": f"{cores * 8 * 32 * H} rollout-steps (bounded sample)"},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
