@@ -40,3 +40,19 @@ def test_errors_are_reported_without_gpu(built):
     assert b"null engine" in lib.spi_last_error()
     rc = lib.spi_create(None, None)
     assert rc == -1
+
+
+def test_kernel_variant_and_fisher_entry_points_validate_arguments(built):
+    """Null handles and out-of-range arguments come back as SPI_EINVAL before any CUDA call."""
+    import ctypes
+    from spi_gb300 import _lib
+    from spi_gb300.server import _bind
+    lib = _lib.engine_lib()
+    assert lib.spi_set_kernel_layout(None, 1) == -1
+    assert lib.spi_set_kernel_config(None, 3) == -1
+    assert lib.spi_fisher_ex(None, 1, 1, 13, None, ctypes.c_double(0.0), 1, None, None, None, None) == -1
+    assert b"spi_fisher" in lib.spi_last_error()
+    assert lib.spi_fisher_ex(None, 1, 1, 14, None, ctypes.c_double(0.0), 0, None, None, None, None) == -1
+    srv = _bind(ctypes.CDLL(lib._name))
+    assert srv.spi_server_set_kernel_layout(None, 1) == -1
+    assert srv.spi_server_set_kernel_config(None, 3) == -1
