@@ -175,7 +175,7 @@ def served_vs_plain(specs, realtime, cfg=None, variant="lane3"):
     ratios = np.array(ratios)
     out = {}
     for name, r in (("served", served), ("plain", plain)):
-        out[name] = {k: v for k, v in r.items() if k != "results"}
+        out[name] = {k: v for k, v in r.items() if k not in ("results", "latencies")}
     out["speedup_rollout_steps"] = served["rollout_steps_per_s"] / plain["rollout_steps_per_s"]
     # Correctness at the 1e-4 relative cost bar: one CEM iteration per job, served and plain. Both
     # paths score the same seeded prior population, so their best costs are comparable directly.

@@ -257,9 +257,13 @@ int spi_server_poll(spi_server* s, spi_job_result* results, int max, int32_t* n_
 int spi_server_wait(spi_server* s);
 /* Active job count and free budget. */
 int spi_server_stats(spi_server* s, int32_t* active, size_t* bytes_free);
-/* Admission cap on rollout work per tick, in (theta, 8-window group) items summed over active
- * jobs (0 = no cap). A job that would exceed it waits (SPI_EBUDGET) unless nothing is active:
- * once the GPU is full, admitting more jobs only slows every job down. */
+/* Cap on rollout work per tick, in work items (theta x 8-window group in the quad layout,
+ * theta x 32-window block in the lane layout; 0 = no cap). Admission depends only on slots and
+ * the HBM budget; each tick then runs the admitted jobs with the least remaining work
+ * (remaining iterations x work items x horizon) first, as many as fit the cap (at least one),
+ * and the others stay resident until they are among the shortest. Once the GPU is full,
+ * running more jobs at once only slows each of them down; shortest-remaining-work order
+ * lets a short job that arrives during a long one finish first. */
 int spi_server_set_work_cap(spi_server* s, long long max_items);
 /* Persistent-grid shape: CTAs per SM (0 = occupancy maximum) and work items claimed per atomic. */
 int spi_server_config(spi_server* s, int ctas_per_sm, int items_per_claim);
@@ -270,6 +274,11 @@ int spi_server_set_kernel_config(spi_server* s, int min_blocks);
  * SPI_LAYOUT_LANE (one lane per rollout, work items of 32 windows; min_blocks 2 or 3), as
  * spi_set_kernel_layout. Only while no job is held (SPI_ESTATE otherwise). */
 int spi_server_set_kernel_layout(spi_server* s, int layout);
+/* CEM-iteration rounds per tick (1..8, default 1). Each tick runs this many rounds of one
+ * iteration (sample, rollout, finalize, refit); a job takes part in as many rounds as the
+ * largest active job's work per iteration (work items x horizon) is a multiple of its own,
+ * capped by its remaining iterations, so small jobs advance several iterations per tick. */
+int spi_server_set_rounds(spi_server* s, int rounds);
 
 /* ---- evaluation without any device allocation ---------------------------------------
  * No counterpart in the reference. For callers that must not let a library call cudaMalloc:

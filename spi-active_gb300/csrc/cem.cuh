@@ -40,10 +40,13 @@ __device__ __forceinline__ unsigned long long cost_key(float c, unsigned idx) {
 }
 
 // Draw the population of the current iteration into st->theta; one grid row per state.
-static __global__ void cem_sample_kernel(const CemState* __restrict__ st_all) {
+// rounds (optional, one per state): a state takes part only while round < rounds[state].
+static __global__ void cem_sample_kernel(const CemState* __restrict__ st_all, const int* __restrict__ rounds = nullptr,
+                                         int round = 0) {
   const CemState* st = st_all + blockIdx.y;
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (!st->active || n >= st->n_samples) return;
+  if (rounds && round >= rounds[blockIdx.y]) return;
   float* theta = st->theta + (size_t)n * SPI_THETA_DIM;
   const int P = st->dim, it = st->iter;
   const uint32_t k0 = (uint32_t)(st->seed & 0xFFFFFFFFull), k1 = (uint32_t)(st->seed >> 32);
@@ -95,8 +98,12 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
-// One CTA (1024 threads) per state: elite select + mean / covariance + Cholesky.
-static __global__ void __launch_bounds__(1024) cem_refit_kernel(CemState* __restrict__ st_all) {
+// One CTA (1024 threads) per state: elite select + mean / covariance + Cholesky. rounds as
+// in cem_sample_kernel.
+static __global__ void __launch_bounds__(1024) cem_refit_kernel(CemState* __restrict__ st_all,
+                                                               const int* __restrict__ rounds = nullptr,
+                                                               int round = 0) {
+  if (rounds && round >= rounds[blockIdx.x]) return;   // uniform per CTA, before any barrier
   extern __shared__ unsigned long long keys[];
   __shared__ double s_mu[CEM_MAX_DIM];
   __shared__ double s_cov[CEM_MAX_DIM * CEM_MAX_DIM];

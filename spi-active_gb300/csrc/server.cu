@@ -33,8 +33,13 @@ struct SlotDesc {
   int N, G;
   float norm;
   int active;
-  long long warp_begin;
 };
+
+// A tick runs up to kMaxRounds rounds of one CEM iteration each (sample, rollout, finalize,
+// refit); slot j takes part in rounds 0 .. rounds[j] - 1, so jobs with less work per
+// iteration advance several iterations per tick. Per round the rollout's work items are
+// laid out slot after slot (begin[round][slot]) in the order order[round][0 .. n_order).
+constexpr int kMaxRounds = 8;
 
 struct TickInfo {
   long long total;   // work items this tick
@@ -78,14 +83,20 @@ __global__ void srv_fill(float* p, float v, int n) {
 template <int MINB>
 __global__ void __launch_bounds__(128, MINB) server_rollout_kernel(const DevModel* __restrict__ model,
                                                              const SlotDesc* __restrict__ slots,
-                                                             const int* __restrict__ order,
-                                                             const TickInfo* __restrict__ info,
-                                                             unsigned long long* __restrict__ counter,
-                                                             unsigned long long* __restrict__ n_bad) {
+                                                             const int* __restrict__ order_all,
+                                                             const long long* __restrict__ begin_all,
+                                                             const TickInfo* __restrict__ info_all,
+                                                             unsigned long long* __restrict__ counter_all,
+                                                             unsigned long long* __restrict__ n_bad,
+                                                             int max_slots, int round) {
   __shared__ DevModel M;
   load_model_smem(&M, model);
   __syncthreads();
   const int lane = threadIdx.x & 31;
+  const TickInfo* info = info_all + round;
+  const int* order = order_all + (size_t)round * max_slots;
+  const long long* begin = begin_all + (size_t)round * max_slots;
+  unsigned long long* counter = counter_all + round;
   const long long total = info->total;
   const int n_order = info->n_order, per = info->items_per_claim;
   while (true) {
@@ -99,10 +110,10 @@ __global__ void __launch_bounds__(128, MINB) server_rollout_kernel(const DevMode
       int lo = 0, hi = n_order - 1;   // last slot whose range starts at or before item
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (slots[order[mid]].warp_begin <= item) lo = mid; else hi = mid - 1;
+        if (begin[order[mid]] <= item) lo = mid; else hi = mid - 1;
       }
       const SlotDesc& S = slots[order[lo]];
-      const long long local = item - S.warp_begin;
+      const long long local = item - begin[order[lo]];
       const int n = (int)(local / S.G), g = (int)(local % S.G);
       rollout_group<false>(M, S.win, S.theta + (size_t)n * SPI_THETA_DIM, g,
                            S.partial + ((size_t)n * S.G + g) * SPI_N_COMP, nullptr, n_bad);
@@ -116,14 +127,20 @@ __global__ void __launch_bounds__(128, MINB) server_rollout_kernel(const DevMode
 template <int MINB>
 __global__ void __launch_bounds__(128, MINB) server_rollout_lane_kernel(const __grid_constant__ DevModel M,
                                                                   const SlotDesc* __restrict__ slots,
-                                                                  const int* __restrict__ order,
-                                                                  const TickInfo* __restrict__ info,
-                                                                  unsigned long long* __restrict__ counter,
-                                                                  unsigned long long* __restrict__ n_bad) {
+                                                                  const int* __restrict__ order_all,
+                                                                  const long long* __restrict__ begin_all,
+                                                                  const TickInfo* __restrict__ info_all,
+                                                                  unsigned long long* __restrict__ counter_all,
+                                                                  unsigned long long* __restrict__ n_bad,
+                                                                  int max_slots, int round) {
   extern __shared__ float lane_smem[];               // kLaneParkBytes
   __shared__ BaseParams<float> bp_warp[4];
   __shared__ LegParams<float> lp_warp[4][2];
   const int lane = threadIdx.x & 31;
+  const TickInfo* info = info_all + round;
+  const int* order = order_all + (size_t)round * max_slots;
+  const long long* begin = begin_all + (size_t)round * max_slots;
+  unsigned long long* counter = counter_all + round;
   const long long total = info->total;
   const int n_order = info->n_order, per = info->items_per_claim;
   while (true) {
@@ -137,10 +154,10 @@ __global__ void __launch_bounds__(128, MINB) server_rollout_lane_kernel(const __
       int lo = 0, hi = n_order - 1;   // last slot whose range starts at or before item
       while (lo < hi) {
         const int mid = (lo + hi + 1) >> 1;
-        if (slots[order[mid]].warp_begin <= item) lo = mid; else hi = mid - 1;
+        if (begin[order[mid]] <= item) lo = mid; else hi = mid - 1;
       }
       const SlotDesc& S = slots[order[lo]];
-      const long long local = item - S.warp_begin;
+      const long long local = item - begin[order[lo]];
       const int WB = (S.win.W + 31) >> 5;
       const int n = (int)(local / WB), wb = (int)(local % WB);
       rollout_lane_warp<false>(M, S.win, S.theta + (size_t)n * SPI_THETA_DIM, wb,
@@ -149,11 +166,11 @@ __global__ void __launch_bounds__(128, MINB) server_rollout_lane_kernel(const __
   }
 }
 
-__global__ void server_finalize_kernel(const SlotDesc* __restrict__ slots, int mode, float w0, float w1, float w2,
-                                       float w3, float w4, float w5) {
+__global__ void server_finalize_kernel(const SlotDesc* __restrict__ slots, const int* __restrict__ rounds, int round,
+                                       int mode, float w0, float w1, float w2, float w3, float w4, float w5) {
   const SlotDesc& S = slots[blockIdx.y];
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (!S.active || n >= S.N) return;
+  if (!S.active || n >= S.N || round >= rounds[blockIdx.y]) return;
   const float w[6] = {w0, w1, w2, w3, w4, w5};
   finalize_one(S.partial, n, S.G, S.norm, mode, w, S.comp, S.cost);
 }
@@ -191,11 +208,15 @@ struct spi_server {
   std::vector<SlotHost> slots;
   SlotDesc* d_slots = nullptr;
   SlotDesc* h_slots = nullptr;     // pinned staging
-  int* d_order = nullptr;
+  int* d_order = nullptr;          // [kMaxRounds][max_slots]
   int* h_order = nullptr;          // pinned
-  TickInfo* d_info = nullptr;
+  long long* d_begin = nullptr;    // [kMaxRounds][max_slots]
+  long long* h_begin = nullptr;    // pinned
+  int* d_rounds = nullptr;         // [max_slots]
+  int* h_rounds = nullptr;         // pinned
+  TickInfo* d_info = nullptr;      // [kMaxRounds]
   TickInfo* h_info = nullptr;      // pinned
-  unsigned long long* d_counter = nullptr;
+  unsigned long long* d_counter = nullptr;   // [kMaxRounds]
   unsigned long long* d_bad = nullptr;
   CemState* d_cem = nullptr;
   CemState* h_cem_in = nullptr;    // pinned, per slot
@@ -208,6 +229,7 @@ struct spi_server {
   long long max_items = 0;         // admission cap on work items per tick (0: none)
   int min_blocks = 3;              // rollout kernel occupancy variant
   int layout = SPI_LAYOUT_QUAD;    // SPI_LAYOUT_QUAD or SPI_LAYOUT_LANE
+  int rounds = 1;                  // CEM-iteration rounds per tick (1 .. kMaxRounds)
   int cost_mode = 1;
   float sq_w[6] = {10.f, 5.f, 0.1f, 0.1f, 1.f, 0.01f};
   long long ticks = 0;
@@ -240,36 +262,41 @@ void free_server(spi_server* s) {
   for (auto& ev : s->tick_done) if (ev) cudaEventDestroy(ev);
   if (s->capture) cudaStreamDestroy(s->capture);
   cudaFree(s->d_model); cudaFree(s->d_slots); cudaFree(s->d_order); cudaFree(s->d_info);
+  cudaFree(s->d_begin); cudaFree(s->d_rounds);
   cudaFree(s->d_counter); cudaFree(s->d_bad); cudaFree(s->d_cem);
   cudaFreeHost(s->h_slots); cudaFreeHost(s->h_order); cudaFreeHost(s->h_info);
+  cudaFreeHost(s->h_begin); cudaFreeHost(s->h_rounds);
   cudaFreeHost(s->h_cem_in); cudaFreeHost(s->h_cem_out); cudaFreeHost(s->h_zero);
   delete s;
 }
 
 int enqueue_tick(spi_server* s) {
   const int rows = (s->max_samples + 127) / 128;
-  cudaError_t ce = cudaMemsetAsync(s->d_counter, 0, sizeof(unsigned long long), s->stream);
-  if (ce != cudaSuccess) return cuda_error(ce, "tick: reset counter");
-  cem_sample_kernel<<<dim3(rows, s->max_slots), 128, 0, s->stream>>>(s->d_cem);
-  if (s->layout == SPI_LAYOUT_LANE) {
-    if (s->min_blocks <= 2)
-      server_rollout_lane_kernel<2><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
-          s->host_model, s->d_slots, s->d_order, s->d_info, s->d_counter, s->d_bad);
-    else
-      server_rollout_lane_kernel<3><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
-          s->host_model, s->d_slots, s->d_order, s->d_info, s->d_counter, s->d_bad);
-  } else if (s->min_blocks == 4)
-    server_rollout_kernel<4><<<s->grid, 128, 0, s->stream>>>(s->d_model, s->d_slots, s->d_order, s->d_info,
-                                                             s->d_counter, s->d_bad);
-  else
-    server_rollout_kernel<3><<<s->grid, 128, 0, s->stream>>>(s->d_model, s->d_slots, s->d_order, s->d_info,
-                                                             s->d_counter, s->d_bad);
-  const float* w = s->sq_w;
-  server_finalize_kernel<<<dim3(rows, s->max_slots), 128, 0, s->stream>>>(s->d_slots, s->cost_mode, w[0], w[1],
-                                                                          w[2], w[3], w[4], w[5]);
+  cudaError_t ce = cudaMemsetAsync(s->d_counter, 0, sizeof(unsigned long long) * kMaxRounds, s->stream);
+  if (ce != cudaSuccess) return cuda_error(ce, "tick: reset counters");
   int npad = 1;
   while (npad < s->max_samples) npad <<= 1;
-  cem_refit_kernel<<<s->max_slots, 1024, npad * sizeof(unsigned long long), s->stream>>>(s->d_cem);
+  const float* w = s->sq_w;
+  for (int r = 0; r < s->rounds; ++r) {
+    cem_sample_kernel<<<dim3(rows, s->max_slots), 128, 0, s->stream>>>(s->d_cem, s->d_rounds, r);
+    if (s->layout == SPI_LAYOUT_LANE) {
+      if (s->min_blocks <= 2)
+        server_rollout_lane_kernel<2><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
+            s->host_model, s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
+      else
+        server_rollout_lane_kernel<3><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
+            s->host_model, s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
+    } else if (s->min_blocks == 4) {
+      server_rollout_kernel<4><<<s->grid, 128, 0, s->stream>>>(s->d_model, s->d_slots, s->d_order, s->d_begin,
+                                                               s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
+    } else {
+      server_rollout_kernel<3><<<s->grid, 128, 0, s->stream>>>(s->d_model, s->d_slots, s->d_order, s->d_begin,
+                                                               s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
+    }
+    server_finalize_kernel<<<dim3(rows, s->max_slots), 128, 0, s->stream>>>(s->d_slots, s->d_rounds, r, s->cost_mode,
+                                                                            w[0], w[1], w[2], w[3], w[4], w[5]);
+    cem_refit_kernel<<<s->max_slots, 1024, npad * sizeof(unsigned long long), s->stream>>>(s->d_cem, s->d_rounds, r);
+  }
   ce = cudaGetLastError();
   return ce == cudaSuccess ? SPI_OK : cuda_error(ce, "tick: launch");
 }
@@ -342,17 +369,22 @@ int spi_server_create(const spi_robot* robot, int max_slots, int max_samples, si
   SRV_TRY(cudaMemcpy(s->d_model, &s->host_model, sizeof(DevModel), cudaMemcpyHostToDevice));
   SRV_TRY(cudaMalloc(&s->d_slots, sizeof(SlotDesc) * max_slots));
   SRV_TRY(cudaMemset(s->d_slots, 0, sizeof(SlotDesc) * max_slots));
-  SRV_TRY(cudaMalloc(&s->d_order, sizeof(int) * max_slots));
-  SRV_TRY(cudaMalloc(&s->d_info, sizeof(TickInfo)));
-  SRV_TRY(cudaMemset(s->d_info, 0, sizeof(TickInfo)));
-  SRV_TRY(cudaMalloc(&s->d_counter, sizeof(unsigned long long)));
+  SRV_TRY(cudaMalloc(&s->d_order, sizeof(int) * max_slots * kMaxRounds));
+  SRV_TRY(cudaMalloc(&s->d_begin, sizeof(long long) * max_slots * kMaxRounds));
+  SRV_TRY(cudaMalloc(&s->d_rounds, sizeof(int) * max_slots));
+  SRV_TRY(cudaMemset(s->d_rounds, 0, sizeof(int) * max_slots));
+  SRV_TRY(cudaMalloc(&s->d_info, sizeof(TickInfo) * kMaxRounds));
+  SRV_TRY(cudaMemset(s->d_info, 0, sizeof(TickInfo) * kMaxRounds));
+  SRV_TRY(cudaMalloc(&s->d_counter, sizeof(unsigned long long) * kMaxRounds));
   SRV_TRY(cudaMalloc(&s->d_bad, sizeof(unsigned long long)));
   SRV_TRY(cudaMemset(s->d_bad, 0, sizeof(unsigned long long)));
   SRV_TRY(cudaMalloc(&s->d_cem, sizeof(CemState) * max_slots));
   SRV_TRY(cudaMemset(s->d_cem, 0, sizeof(CemState) * max_slots));
   SRV_TRY(cudaMallocHost(&s->h_slots, sizeof(SlotDesc) * max_slots));
-  SRV_TRY(cudaMallocHost(&s->h_order, sizeof(int) * max_slots));
-  SRV_TRY(cudaMallocHost(&s->h_info, sizeof(TickInfo)));
+  SRV_TRY(cudaMallocHost(&s->h_order, sizeof(int) * max_slots * kMaxRounds));
+  SRV_TRY(cudaMallocHost(&s->h_begin, sizeof(long long) * max_slots * kMaxRounds));
+  SRV_TRY(cudaMallocHost(&s->h_rounds, sizeof(int) * max_slots));
+  SRV_TRY(cudaMallocHost(&s->h_info, sizeof(TickInfo) * kMaxRounds));
   SRV_TRY(cudaMallocHost(&s->h_cem_in, sizeof(CemState) * max_slots));
   SRV_TRY(cudaMallocHost(&s->h_cem_out, sizeof(CemState) * max_slots));
   SRV_TRY(cudaMallocHost(&s->h_zero, sizeof(int)));
@@ -415,6 +447,15 @@ int spi_server_set_kernel_config(spi_server* s, int min_blocks) {
   return resize_grid(s);
 }
 
+int spi_server_set_rounds(spi_server* s, int rounds) {
+  if (!s) return set_error(SPI_EINVAL, "null server");
+  if (rounds < 1 || rounds > kMaxRounds)
+    return set_error(SPI_EINVAL, "spi_server_set_rounds: rounds %d outside [1, %d]", rounds, kMaxRounds);
+  s->rounds = rounds;
+  if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+  return SPI_OK;
+}
+
 int spi_server_set_kernel_layout(spi_server* s, int layout) {
   if (!s) return set_error(SPI_EINVAL, "null server");
   if (layout != SPI_LAYOUT_QUAD && layout != SPI_LAYOUT_LANE)
@@ -454,16 +495,6 @@ int spi_server_submit(spi_server* s, const spi_job* job, int32_t* slot_out) {
   if (slot < 0 || s->used + L.total > s->budget)
     return set_error(SPI_EBUDGET, "spi_server_submit: %s (need %zu bytes, %zu free)",
                      slot < 0 ? "no free slot" : "over the HBM budget", L.total, s->budget - s->used);
-  if (s->max_items > 0) {
-    long long items = 0;
-    for (const auto& o : s->slots)
-      if (o.active) items += slot_items(s, o.desc);
-    const long long mine =
-        (long long)c.n_samples * (s->layout == SPI_LAYOUT_LANE ? (job->W + 31) / 32 : (job->W + 7) / 8);
-    if (items > 0 && items + mine > s->max_items)
-      return set_error(SPI_EBUDGET, "spi_server_submit: GPU work cap reached (%lld + %lld items > %lld)", items,
-                       mine, s->max_items);
-  }
   CemState& h = s->h_cem_in[slot];
   memset(&h, 0, sizeof(h));
   unsigned seen = 0;
@@ -574,23 +605,62 @@ int spi_server_tick(spi_server* s) {
   });
   cudaError_t ce = cudaEventSynchronize(s->staging_free);   // previous tick's table copies are done
   if (ce != cudaSuccess) return cuda_error(ce, "spi_server_tick: staging");
-  long long begin = 0;
   for (int i = 0; i < s->max_slots; ++i) {
     s->h_slots[i] = s->slots[i].desc;
     s->h_slots[i].active = s->slots[i].active ? 1 : 0;
+    s->h_rounds[i] = 0;
   }
-  for (size_t k = 0; k < act.size(); ++k) {
-    const int i = act[k];
-    s->h_slots[i].warp_begin = begin;
-    begin += slot_items(s, s->h_slots[i]);
-    s->h_order[k] = i;
+  // jobs of this tick: shortest remaining work first (remaining iterations x work items x
+  // horizon), as many as fit the work cap (at least one); the others stay resident and wait
+  auto work = [&](int i) { return slot_items(s, s->h_slots[i]) * (long long)s->h_slots[i].win.H; };
+  std::vector<int> run = act;
+  if (s->max_items > 0) {
+    std::stable_sort(run.begin(), run.end(), [&](int a, int b) {
+      return work(a) * (long long)s->slots[a].remaining < work(b) * (long long)s->slots[b].remaining;
+    });
+    long long items = 0;
+    size_t keep = 0;
+    for (; keep < run.size(); ++keep) {
+      const long long mine = slot_items(s, s->h_slots[run[keep]]);
+      if (keep > 0 && items + mine > s->max_items) break;
+      items += mine;
+    }
+    run.resize(keep);
   }
-  s->h_info->total = begin;
-  s->h_info->n_order = (int)act.size();
-  s->h_info->items_per_claim = s->items_per_claim;
+  // rounds per job: the largest running job's work per iteration over its own, at most the
+  // rounds of a tick and the iterations it has left
+  long long most = 0;
+  for (int i : run) most = std::max(most, work(i));
+  for (int i : run) {
+    const long long mine = std::max(work(i), 1LL);
+    const long long share = std::max(most / mine, 1LL);
+    s->h_rounds[i] = (int)std::min<long long>(std::min<long long>(share, s->rounds), s->slots[i].remaining);
+  }
+  for (int r = 0; r < s->rounds; ++r) {
+    long long begin = 0;
+    int n = 0;
+    int* order = s->h_order + (size_t)r * s->max_slots;
+    long long* beg = s->h_begin + (size_t)r * s->max_slots;
+    for (size_t k = 0; k < act.size(); ++k) {
+      const int i = act[k];
+      beg[i] = begin;
+      if (r >= s->h_rounds[i]) continue;
+      begin += slot_items(s, s->h_slots[i]);
+      order[n++] = i;
+    }
+    s->h_info[r].total = begin;
+    s->h_info[r].n_order = n;
+    s->h_info[r].items_per_claim = s->items_per_claim;
+  }
+  const size_t tab = (size_t)s->rounds * s->max_slots;
   ce = cudaMemcpyAsync(s->d_slots, s->h_slots, sizeof(SlotDesc) * s->max_slots, cudaMemcpyHostToDevice, s->stream);
-  if (ce == cudaSuccess) ce = cudaMemcpyAsync(s->d_order, s->h_order, sizeof(int) * act.size(), cudaMemcpyHostToDevice, s->stream);
-  if (ce == cudaSuccess) ce = cudaMemcpyAsync(s->d_info, s->h_info, sizeof(TickInfo), cudaMemcpyHostToDevice, s->stream);
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(s->d_order, s->h_order, sizeof(int) * tab, cudaMemcpyHostToDevice, s->stream);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync(s->d_begin, s->h_begin, sizeof(long long) * tab, cudaMemcpyHostToDevice, s->stream);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync(s->d_rounds, s->h_rounds, sizeof(int) * s->max_slots, cudaMemcpyHostToDevice, s->stream);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpyAsync(s->d_info, s->h_info, sizeof(TickInfo) * s->rounds, cudaMemcpyHostToDevice, s->stream);
   if (ce == cudaSuccess) ce = cudaEventRecord(s->staging_free, s->stream);
   if (ce != cudaSuccess) return cuda_error(ce, "spi_server_tick: upload table");
   int rc = build_graph(s);
@@ -598,7 +668,7 @@ int spi_server_tick(spi_server* s) {
   ce = cudaGraphLaunch(s->graph, s->stream);
   if (ce == cudaSuccess) ce = cudaEventRecord(s->tick_done[s->ticks & 1], s->stream);
   if (ce != cudaSuccess) return cuda_error(ce, "spi_server_tick: launch");
-  for (int i : act) s->slots[i].remaining -= 1;
+  for (int i : act) s->slots[i].remaining -= s->h_rounds[i];
   ++s->ticks;
   return SPI_OK;
 }

@@ -46,6 +46,7 @@ _API = {
     "spi_server_wait": (ctypes.c_int, [ctypes.c_void_p]),
     "spi_server_set_kernel_config": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "spi_server_set_kernel_layout": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "spi_server_set_rounds": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "spi_server_set_work_cap": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong]),
 }
 
@@ -151,6 +152,10 @@ class Server:
     def set_kernel_layout(self, layout):
         """0 = quad layout (4 lanes per rollout), 1 = lane layout (one lane per rollout)."""
         _lib.check(self.lib.spi_server_set_kernel_layout(self._h, int(layout)))
+
+    def set_rounds(self, rounds):
+        """CEM-iteration rounds per tick: small jobs take up to this many iterations per tick."""
+        _lib.check(self.lib.spi_server_set_rounds(self._h, int(rounds)))
 
     # rollout-kernel variants the server runs, by the autotuner's names
     VARIANTS = {"quad3": (0, 3), "quad4": (0, 4), "lane2": (1, 2), "lane3": (1, 3)}

@@ -131,6 +131,7 @@ def _summary(specs, latencies, wall, results=None):
     out = {"jobs": len(specs), "rollout_steps": int(steps), "wall_s": wall, "rollout_steps_per_s": steps / wall,
            "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99)),
            "latency_mean_s": float(lat.mean())}
+    out["latencies"] = {s.job_id: float(latencies[s.job_id]) for s in specs}
     if results is not None:
         out["results"] = results
     return out
@@ -143,15 +144,16 @@ def default_work_cap(device=None):
 
 
 def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=64, hbm_budget=150 << 30,
-               ctas_per_sm=0, items_per_claim=1, realtime=True, work_cap=None, variant="lane3"):
+               ctas_per_sm=0, items_per_claim=1, realtime=True, work_cap=None, variant="lane3", rounds=4):
     """Continuous batching: admit on arrival while HBM budget, a slot and GPU work capacity are free;
-    one CEM iteration per tick for every admitted job. Fisher requests are scored on a worker
+    every tick advances each admitted job by 1 .. `rounds` CEM iterations (more for smaller jobs). Fisher requests are scored on a worker
     thread (own engine and stream) while the server keeps ticking; a job completes when its
     score is in."""
     max_samples = max(s.n_samples for s in specs)
     server = Server(cfg, max_slots=max_slots, max_samples=max_samples, hbm_budget_bytes=hbm_budget,
                     device=bank.engine.device)
     server.set_variant(variant)
+    server.set_rounds(rounds)
     server.config(ctas_per_sm, items_per_claim)
     server.set_work_cap(default_work_cap(bank.engine.device) if work_cap is None else work_cap)
     jobs = {}
@@ -160,6 +162,8 @@ def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=
         jobs[s.job_id] = (Server.make_job(init, act, tgt, _cem_cfg(s), s.iterations), (init, act, tgt))
     pending = sorted(specs, key=lambda s: s.arrival)
     scorer = FisherScorer(cfg, device=bank.engine.device, own_stream=True) if any(s.fisher for s in specs) else None
+    if scorer is not None:
+        scorer.score(THETA_NOMINAL)       # first-call setup (allocations, attributes) before the clock
     pool = ThreadPoolExecutor(max_workers=1) if scorer is not None else None
     by_id = {s.job_id: s for s in specs}
     torch.cuda.synchronize()
@@ -211,6 +215,8 @@ def run_plain(specs, bank: WindowBank, cfg: SimConfig | None = None, graph=True,
     eng = Engine(cfg, device=bank.engine.device)
     set_variant(eng, variant)
     scorer = FisherScorer(cfg, device=bank.engine.device) if any(s.fisher for s in specs) else None
+    if scorer is not None:
+        scorer.score(THETA_NOMINAL)       # first-call setup (allocations, attributes) before the clock
     order = sorted(specs, key=lambda s: s.arrival)
     for s in order:
         bank.get(s)

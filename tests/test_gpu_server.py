@@ -93,3 +93,58 @@ def test_admission_respects_budget_and_slots(built):
     assert s.submit(job3) is None                     # no free slot
     small = Server(max_slots=4, max_samples=64, hbm_budget_bytes=need - 1)
     assert small.submit(job) is None                  # over the HBM budget
+
+
+@pytest.mark.parametrize("variant", ["quad3", "lane3"])
+def test_rounds_per_tick_do_not_change_results(built, variant):
+    """Jobs advanced several CEM iterations per tick reach bitwise the same results."""
+    specs = [(9, 64, 12, 256, [0, 4], 51), (10, 8, 3, 64, [0], 52), (11, 16, 5, 64, [0, 1, 2], 53)]
+    res = {}
+    for rounds in (1, 4):
+        s = _server(variant, max_slots=8, max_samples=256)
+        s.set_rounds(rounds)
+        res[rounds] = _run(s, [_job(*sp, iters=9) for sp in specs])
+    for sp in specs:
+        a, b = res[1][sp[-1]], res[4][sp[-1]]
+        assert a["iterations"] == b["iterations"] == 9
+        assert np.array_equal(a["best_theta"], b["best_theta"]) and a["best_cost"] == b["best_cost"]
+        assert np.array_equal(a["mu"], b["mu"])
+
+
+def test_small_job_takes_several_iterations_per_tick(built):
+    """Beside a job with 64x its work per iteration, a small job takes 4 iterations per tick."""
+    s = _server("lane3", max_slots=4, max_samples=512)
+    s.set_rounds(4)
+    big, keep_big = _job(12, 128, 16, 512, [0, 4], 61, iters=12)
+    small, keep_small = _job(13, 8, 2, 64, [0], 62, iters=12)
+    assert s.submit(big) is not None and s.submit(small) is not None
+    ticks, done = 0, {}
+    while len(done) < 2:
+        s.tick()
+        ticks += 1
+        s.wait()
+        for r in s.poll():
+            done[r["job_id"]] = ticks
+        assert ticks < 40
+    assert done[62] <= 12 // 4 + 2 < done[61]
+
+
+def test_work_cap_runs_shortest_remaining_work_first(built):
+    """Past the work cap jobs wait resident; the job with the least remaining work ticks first."""
+    s = _server("quad3", max_slots=4, max_samples=256)
+    s.set_work_cap(3000)
+    big, keep_big = _job(14, 64, 4, 256, [0], 71, iters=8)       # 256 theta x 8 groups = 2048 items
+    big2, keep_big2 = _job(15, 64, 4, 256, [0], 72, iters=8)
+    assert s.submit(big) is not None
+    s.tick()                                             # job 71 starts alone
+    small, keep_small = _job(16, 8, 4, 32, [0], 73, iters=8)    # 32 items
+    assert s.submit(big2) is not None and s.submit(small) is not None
+    order, ticks = [], 0
+    while len(order) < 3:
+        s.tick()
+        ticks += 1
+        s.wait()
+        order += [r["job_id"] for r in s.poll()]
+        assert ticks < 60
+    # 71 (less remaining than 72) and the small 73 run together; 72 waits for 71
+    assert order.index(73) < order.index(72) and order.index(71) < order.index(72)
