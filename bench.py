@@ -262,6 +262,18 @@ def run_c3(args):
         e1.synchronize()
         fisher_ms[name] = e0.elapsed_time(e1) / 10
     t = float(np.mean(times))
+    # Fisher roofline: J^T Q J over every candidate, 2 x rows x K x K flops per candidate, J read once
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    f_flops = 2.0 * n * wpc * 37 * 13 * 13
+    f_bytes = n * wpc * 37 * 13 * 4
+    f_s = fisher_ms["tensor_cores_bf16"] * 1e-3
+    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    fisher_roof = {"kernel": "fisher_mma_kernel", "bound": "hbm", "achieved": f_bytes / f_s / 1e9, "peak": hbm_peak,
+                   "unit": "GB/s", "frac": f_bytes / f_s / 1e9 / hbm_peak,
+                   "tensor_tflops": f_flops / f_s / 1e12, "tensor_frac": f_flops / f_s / 1e12 / bf16_peak,
+                   "note": "13 x 13 Gram matrices over 296 rows per candidate: too small for either roof "
+                           "(one warp per candidate, latency-bound); peaks from MEASURED_PEAKS.json"}
     tangent_steps = n * wpc * H * 13
     primal_steps = n * (settle + wpc * H)
     line = {"metric": "excitation candidates scored/s", "value": n / t, "unit": "candidates/s", "n_gpus": 1,
@@ -274,7 +286,7 @@ def run_c3(args):
                        "step": "score every candidate once (settle trace, sensitivities, Fisher, log det)"},
             "rollout_steps_per_s": (tangent_steps + primal_steps) / t,
             "tangent_rollout_steps_per_step": tangent_steps, "primal_rollout_steps_per_step": primal_steps,
-            "fisher_ms": fisher_ms, "best_candidate": int(r["best"]),
+            "fisher_ms": fisher_ms, "fisher_roofline": fisher_roof, "best_candidate": int(r["best"]),
             "logdet_range": [float(np.min(r["logdet"])), float(np.max(r["logdet"]))],
             "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
