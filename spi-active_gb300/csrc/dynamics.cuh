@@ -165,7 +165,9 @@ template <class T> SPI_INL SV<T> mul(const Art<T>& I, const SV<T>& m) {
 // v x* f (force cross product).
 template <class T> SPI_INL SV<T> crf(const SV<T>& v, const SV<T>& f) {
   SV<T> r;
-  r.w = cross(v.w, f.w) + cross(v.v, f.v);
+  const V3<T> a = cross(v.w, f.w);
+  r.w = v3(a.x + v.v.y * f.v.z - v.v.z * f.v.y, a.y + v.v.z * f.v.x - v.v.x * f.v.z,
+           a.z + v.v.x * f.v.y - v.v.y * f.v.x);
   r.v = cross(v.w, f.v);
   return r;
 }
@@ -181,9 +183,33 @@ template <class T> SPI_INL Art<T> rigid(T m, V3<T> h, const S3<T>& Io) {
 }
 // Rigid-body I*v without forming the 6x6.
 template <class T> SPI_INL SV<T> rigid_mul(T m, V3<T> h, const S3<T>& Io, const SV<T>& v) {
+  SV<T> r;   // (Io w + h x v; m v - h x w), each sum one chain of fused multiply-adds
+  const V3<T> iw = mul(Io, v.w);
+  r.w = v3(iw.x + h.y * v.v.z - h.z * v.v.y, iw.y + h.z * v.v.x - h.x * v.v.z, iw.z + h.x * v.v.y - h.y * v.v.x);
+  r.v = v3(m * v.v.x + v.w.y * h.z - v.w.z * h.y, m * v.v.y + v.w.z * h.x - v.w.x * h.z,
+           m * v.v.z + v.w.x * h.y - v.w.y * h.x);
+  return r;
+}
+// Accumulating forms: acc + (product sums), written with the accumulator innermost so that
+// every product fuses into a multiply-add (no separate multiply and final add).
+template <class T> SPI_INL V3<T> mul_acc(const S3<T>& S, V3<T> u, V3<T> acc) {
+  return v3(acc.x + S.xx * u.x + S.xy * u.y + S.xz * u.z,
+            acc.y + S.xy * u.x + S.yy * u.y + S.yz * u.z,
+            acc.z + S.xz * u.x + S.yz * u.y + S.zz * u.z);
+}
+template <class T> SPI_INL V3<T> cross_acc(V3<T> a, V3<T> b, V3<T> acc) {   // acc + a x b
+  return v3(acc.x + a.y * b.z - a.z * b.y, acc.y + a.z * b.x - a.x * b.z, acc.z + a.x * b.y - a.y * b.x);
+}
+template <class T> SPI_INL SV<T> crf_acc(const SV<T>& v, const SV<T>& f, const SV<T>& acc) {   // acc + v x* f
   SV<T> r;
-  r.w = mul(Io, v.w) + cross(h, v.v);
-  r.v = m * v.v - cross(h, v.w);
+  r.w = cross_acc(v.v, f.v, cross_acc(v.w, f.w, acc.w));
+  r.v = cross_acc(v.w, f.v, acc.v);
+  return r;
+}
+template <class T> SPI_INL SV<T> rigid_mul_acc(T m, V3<T> h, const S3<T>& Io, const SV<T>& v, const SV<T>& acc) {
+  SV<T> r;   // acc + I v
+  r.w = cross_acc(h, v.v, mul_acc(Io, v.w, acc.w));
+  r.v = cross_acc(v.w, h, v3(acc.v.x + m * v.v.x, acc.v.y + m * v.v.y, acc.v.z + m * v.v.z));
   return r;
 }
 template <class T> SPI_INL void add_to(Art<T>& a, const Art<T>& b) {
@@ -209,6 +235,9 @@ template <class T> SPI_INL void ri_add_point(RI<T>& a, T mp, V3<T> p) {
   a.I.xy -= hp.x * p.y; a.I.xz -= hp.x * p.z; a.I.yz -= hp.y * p.z;
 }
 template <class T> SPI_INL SV<T> ri_mul(const RI<T>& a, const SV<T>& v) { return rigid_mul(a.m, a.h, a.I, v); }
+template <class T> SPI_INL SV<T> ri_mul_acc(const RI<T>& a, const SV<T>& v, const SV<T>& acc) {
+  return rigid_mul_acc(a.m, a.h, a.I, v, acc);
+}
 // I S for the revolute joint axis AX of the body's own frame: (I e_AX; e_AX x h).
 template <int AX, class T> SPI_INL SV<T> ri_col(const RI<T>& a) {
   SV<T> f;
@@ -238,6 +267,15 @@ template <int RM, class T> SPI_INL V3<T> add_rcross(V3<T> u, V3<T> r, V3<T> w) {
   if (RM == 4) return v3(u.x - r.z * w.y, u.y + r.z * w.x, u.z);
   return u + cross(r, w);
 }
+// acc + R u for the active rotation about AX.
+template <int AX, class T> SPI_INL V3<T> rot_acc(T c, T s, V3<T> u, V3<T> acc) {
+  if (AX == 0) return v3(acc.x + u.x, acc.y + c * u.y - s * u.z, acc.z + s * u.y + c * u.z);
+  return v3(acc.x + c * u.x + s * u.z, acc.y + u.y, acc.z - s * u.x + c * u.z);
+}
+template <int AX, class T> SPI_INL V3<T> rotT_acc(T c, T s, V3<T> u, V3<T> acc) {
+  if (AX == 0) return v3(acc.x + u.x, acc.y + c * u.y + s * u.z, acc.z - s * u.y + c * u.z);
+  return v3(acc.x + c * u.x - s * u.z, acc.y + u.y, acc.z + s * u.x + c * u.z);
+}
 // X^T f: child force to parent coordinates.
 template <int AX, int RM = 7, class T> SPI_INL SV<T> force_to_parent(const SV<T>& f, T c, T s, V3<T> r) {
   SV<T> o;
@@ -245,11 +283,84 @@ template <int AX, int RM = 7, class T> SPI_INL SV<T> force_to_parent(const SV<T>
   o.w = add_rcross<RM>(rot<AX>(c, s, f.w), r, o.v);
   return o;
 }
+// acc + X^T f.
+template <int AX, int RM = 7, class T>
+SPI_INL SV<T> force_to_parent_acc(const SV<T>& f, T c, T s, V3<T> r, const SV<T>& acc) {
+  SV<T> o;
+  const V3<T> fv = rot<AX>(c, s, f.v);
+  o.v = acc.v + fv;
+  o.w = add_rcross<RM>(rot_acc<AX>(c, s, f.w, acc.w), r, fv);
+  return o;
+}
 // X m: parent motion to child coordinates.
 template <int AX, int RM = 7, class T> SPI_INL SV<T> motion_to_child(const SV<T>& m, T c, T s, V3<T> r) {
   SV<T> o;
   o.w = rotT<AX>(c, s, m.w);
   o.v = rotT<AX>(c, s, sub_rcross<RM>(m.v, r, m.w));
+  return o;
+}
+// acc + X m.
+template <int AX, int RM = 7, class T>
+SPI_INL SV<T> motion_to_child_acc(const SV<T>& m, T c, T s, V3<T> r, const SV<T>& acc) {
+  SV<T> o;
+  o.w = rotT_acc<AX>(c, s, m.w, acc.w);
+  o.v = rotT_acc<AX>(c, s, sub_rcross<RM>(m.v, r, m.w), acc.v);
+  return o;
+}
+
+// base + R M R^T for symmetric M and the active plane rotation R about AX (rot_sym with the
+// parent's own inertia as accumulator).
+template <int AX, class T> SPI_INL S3<T> rot_sym_acc(T c, T s, const S3<T>& M, const S3<T>& base) {
+  S3<T> r;
+  const T cc = c * c, ss = s * s, cs = c * s, cs2 = T(2) * cs;
+  if (AX == 1) {
+    r.xx = base.xx + cc * M.xx + cs2 * M.xz + ss * M.zz;
+    r.zz = base.zz + ss * M.xx - cs2 * M.xz + cc * M.zz;
+    r.xz = base.xz + cs * (M.zz - M.xx) + (cc - ss) * M.xz;
+    r.xy = base.xy + c * M.xy + s * M.yz;
+    r.yz = base.yz - s * M.xy + c * M.yz;
+    r.yy = base.yy + M.yy;
+  } else {
+    r.yy = base.yy + cc * M.yy - cs2 * M.yz + ss * M.zz;
+    r.zz = base.zz + ss * M.yy + cs2 * M.yz + cc * M.zz;
+    r.yz = base.yz + cs * (M.yy - M.zz) + (cc - ss) * M.yz;
+    r.xy = base.xy + c * M.xy - s * M.xz;
+    r.xz = base.xz + s * M.xy + c * M.xz;
+    r.xx = base.xx + M.xx;
+  }
+  return r;
+}
+// base + X^T I X: ri_to_parent with the parent body's own inertia as accumulator.
+template <int AX, int RM, class T> SPI_INL RI<T> ri_to_parent_acc(const RI<T>& c, T cs, T sn, V3<T> r, const RI<T>& base) {
+  RI<T> o;
+  o.m = base.m + c.m;
+  const S3<T> I1 = rot_sym_acc<AX>(cs, sn, c.I, base.I);
+  const V3<T> a = rot<AX>(cs, sn, c.h);
+  if (RM == 4) {   // r = (0, 0, z)
+    const T z = r.z, mz = c.m * z;
+    const T t = T(2) * a.z + mz;
+    o.h = v3(base.h.x + a.x, base.h.y + a.y, base.h.z + a.z + mz);
+    o.I.xx = I1.xx + z * t; o.I.yy = I1.yy + z * t; o.I.zz = I1.zz;
+    o.I.xy = I1.xy; o.I.xz = I1.xz - a.x * z; o.I.yz = I1.yz - a.y * z;
+    return o;
+  }
+  if (RM == 2) {   // r = (0, y, 0)
+    const T y = r.y, my = c.m * y;
+    const T t = T(2) * a.y + my;
+    o.h = v3(base.h.x + a.x, base.h.y + a.y + my, base.h.z + a.z);
+    o.I.xx = I1.xx + y * t; o.I.yy = I1.yy; o.I.zz = I1.zz + y * t;
+    o.I.xy = I1.xy - a.x * y; o.I.xz = I1.xz; o.I.yz = I1.yz - a.z * y;
+    return o;
+  }
+  const V3<T> mr = c.m * r;
+  o.h = base.h + a + mr;
+  const T ax = a.x * r.x, ay = a.y * r.y, az = a.z * r.z;
+  o.I.xx = I1.xx + T(2) * (ay + az) + mr.y * r.y + mr.z * r.z;
+  o.I.yy = I1.yy + T(2) * (ax + az) + mr.x * r.x + mr.z * r.z;
+  o.I.zz = I1.zz + T(2) * (ax + ay) + mr.x * r.x + mr.y * r.y;
+  o.I.xy = I1.xy - (a.x * r.y + a.y * r.x) - mr.x * r.y;
+  o.I.xz = I1.xz - (a.x * r.z + a.z * r.x) - mr.x * r.z;
+  o.I.yz = I1.yz - (a.y * r.z + a.z * r.y) - mr.y * r.z;
   return o;
 }
 
@@ -487,15 +598,16 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
               cb2 = vel_product<1>(v2, L.qd[2]);
   // foot: position and velocity, calf -> thigh -> hip -> base -> world
   V3<T> fc = v3(T(M.foot[0]), T(M.foot[1]), T(M.foot[2]));
-  V3<T> vf = v2.v + cross(v2.w, fc);
-  V3<T> pf = rot<1>(C[2], S[2], fc) + r2;
+  V3<T> vf = cross_acc(v2.w, fc, v2.v);
+  V3<T> pf = rot_acc<1>(C[2], S[2], fc, r2);
   vf = rot<1>(C[2], S[2], vf);
-  pf = rot<1>(C[1], S[1], pf) + r1;
+  pf = rot_acc<1>(C[1], S[1], pf, r1);
   vf = rot<1>(C[1], S[1], vf);
-  pf = rot<0>(C[0], S[0], pf) + r0;
+  pf = rot_acc<0>(C[0], S[0], pf, r0);
   vf = rot<0>(C[0], S[0], vf);
   T mimp;
-  V3<T> F = contact_force(M, T(M.foot_r), B.p.z + dot(row(B.R, 2), pf), mul(B.R, vf), &mimp);
+  V3<T> F = contact_force(M, T(M.foot_r),
+                          B.p.z + B.R.m[2][0] * pf.x + B.R.m[2][1] * pf.y + B.R.m[2][2] * pf.z, mul(B.R, vf), &mimp);
   // the implicit point mass acts on the true acceleration while the dynamics run in the
   // gravity-shifted frame: its share of the shift enters as a force mimp*g upwards
   F.z = F.z + mimp * T(M.g);
@@ -507,26 +619,24 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
   const RI<T> Ical = leg_ri<T>(M, 2, leg);
   RI<T> Rc2 = Ical;
   ri_add_point(Rc2, mimp, fc);
-  RI<T> Rc1 = leg_ri<T>(M, 1, leg);
-  ri_add(Rc1, ri_to_parent<1, 4>(Rc2, C[2], S[2], r2));
-  RI<T> Rc0 = leg_ri<T>(M, 0, leg);
-  ri_add(Rc0, ri_to_parent<1, 2>(Rc1, C[1], S[1], r1));
+  const RI<T> Rc1 = ri_to_parent_acc<1, 4>(Rc2, C[2], S[2], r2, leg_ri<T>(M, 1, leg));
+  const RI<T> Rc0 = ri_to_parent_acc<1, 2>(Rc1, C[1], S[1], r1, leg_ri<T>(M, 0, leg));
   // bias pass (a0 = 0, qdd = 0): accelerations are the accumulated velocity products; the
   // implicit point mass takes part in the inertial force, not in the velocity term
-  const SV<T> ab1 = motion_to_child<1, 2>(cb0, C[1], S[1], r1) + cb1;
-  const SV<T> ab2 = motion_to_child<1, 4>(ab1, C[2], S[2], r2) + cb2;
-  SV<T> f2 = crf(v2, ri_mul(Ical, v2)) + ri_mul(Rc2, ab2);
-  f2.w = f2.w - cross(fc, Fc);
+  const SV<T> ab1 = motion_to_child_acc<1, 2>(cb0, C[1], S[1], r1, cb1);
+  const SV<T> ab2 = motion_to_child_acc<1, 4>(ab1, C[2], S[2], r2, cb2);
+  SV<T> f2 = ri_mul_acc(Rc2, ab2, crf(v2, ri_mul(Ical, v2)));
+  f2.w = cross_acc(Fc, fc, f2.w);
   f2.v = f2.v - Fc;
   SV<T> f1;
   {
     const RI<T> Ith = leg_ri<T>(M, 1, leg);
-    f1 = force_to_parent<1, 4>(f2, C[2], S[2], r2) + (crf(v1, ri_mul(Ith, v1)) + ri_mul(Ith, ab1));
+    f1 = ri_mul_acc(Ith, ab1, crf_acc(v1, ri_mul(Ith, v1), force_to_parent<1, 4>(f2, C[2], S[2], r2)));
   }
   SV<T> f0;
   {
     const RI<T> Ihp = leg_ri<T>(M, 0, leg);
-    f0 = force_to_parent<1, 2>(f1, C[1], S[1], r1) + (crf(v0, ri_mul(Ihp, v0)) + ri_mul(Ihp, cb0));
+    f0 = ri_mul_acc(Ihp, cb0, crf_acc(v0, ri_mul(Ihp, v0), force_to_parent<1, 2>(f1, C[1], S[1], r1)));
   }
   const SV<T> pc = force_to_parent<0, 7>(f0, C[0], S[0], r0);
   // joint force columns F_k = I_k^c S_k in base coordinates, and the joint-space inertia
@@ -561,7 +671,10 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
   art_sub_outer(out.I, Kp0, K0);
   art_sub_outer(out.I, Kp1, K1);
   art_sub_outer(out.I, Kp2, K2);
-  out.p = pc + (y0 * K0 + (y1 * K1 + y2 * K2));
+  out.p.w = v3(pc.w.x + y2 * K2.w.x + y1 * K1.w.x + y0 * K0.w.x, pc.w.y + y2 * K2.w.y + y1 * K1.w.y + y0 * K0.w.y,
+               pc.w.z + y2 * K2.w.z + y1 * K1.w.z + y0 * K0.w.z);
+  out.p.v = v3(pc.v.x + y2 * K2.v.x + y1 * K1.v.x + y0 * K0.v.x, pc.v.y + y2 * K2.v.y + y1 * K1.v.y + y0 * K0.v.y,
+               pc.v.z + y2 * K2.v.z + y1 * K1.v.z + y0 * K0.v.z);
   // two of the eight base-box corners; a corner can only reach the ground when the base origin
   // is lower than the box's half-diagonal, so a warp whose rollouts are all higher skips them
   // (a corner off the ground adds exactly zero force and zero implicit mass)
@@ -570,12 +683,13 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
     for (int j = 0; j < 2; ++j) {
       const float* cc = M.corner[2 * leg + j];
       V3<T> rc = v3(T(cc[0]), T(cc[1]), T(cc[2]));
-      V3<T> vc = B.nu.v + cross(B.nu.w, rc);
+      V3<T> vc = cross_acc(B.nu.w, rc, B.nu.v);
       T mc;
-      V3<T> Fw = contact_force(M, T(0), B.p.z + dot(row(B.R, 2), rc), mul(B.R, vc), &mc);
+      V3<T> Fw = contact_force(M, T(0), B.p.z + B.R.m[2][0] * rc.x + B.R.m[2][1] * rc.y + B.R.m[2][2] * rc.z,
+                               mul(B.R, vc), &mc);
       Fw.z = Fw.z + mc * T(M.g);
       V3<T> Fb = mulT(B.R, Fw);
-      out.p.w = out.p.w - cross(rc, Fb);
+      out.p.w = cross_acc(Fb, rc, out.p.w);
       out.p.v = out.p.v - Fb;
       add_point_mass(out.I, mc, rc);
     }
@@ -591,9 +705,7 @@ template <class T>
 SPI_INL SV<T> phase_b(const DevModel& M, const BaseParams<T>& bp, const LegOut<T>& sum, BaseState<T>& B) {
   Art<T> IA = rigid(bp.m, bp.h, bp.Io);
   add_to(IA, sum.I);
-  SV<T> pA = crf(B.nu, rigid_mul(bp.m, bp.h, bp.Io, B.nu));
-  pA.w = pA.w + sum.p.w;
-  pA.v = pA.v + sum.p.v;
+  const SV<T> pA = crf_acc(B.nu, rigid_mul(bp.m, bp.h, bp.Io, B.nu), sum.p);
   // 6x6 symmetric matrix in (w; v) order, Cholesky L L^T, solve IA a = -pA
   T Mx[6][6];
   Mx[0][0] = IA.A.xx; Mx[1][1] = IA.A.yy; Mx[2][2] = IA.A.zz;
@@ -662,9 +774,14 @@ SPI_INL SV<T> phase_b(const DevModel& M, const BaseParams<T>& bp, const LegOut<T
 template <class T, class WK>
 SPI_INL void phase_c(const DevModel& M, int leg, const SV<T>& a0, const WK& W, LegState<T>& L) {
   (void)leg;
-  const T w0 = W.y[0] - (dot(W.Kp[0].w, a0.w) + dot(W.Kp[0].v, a0.v));
-  const T w1 = W.y[1] - (dot(W.Kp[1].w, a0.w) + dot(W.Kp[1].v, a0.v));
-  const T w2 = W.y[2] - (dot(W.Kp[2].w, a0.w) + dot(W.Kp[2].v, a0.v));
+  T w[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const SV<T>& q = W.Kp[k];
+    w[k] = W.y[k] - q.w.x * a0.w.x - q.w.y * a0.w.y - q.w.z * a0.w.z - q.v.x * a0.v.x - q.v.y * a0.v.y -
+           q.v.z * a0.v.z;
+  }
+  const T w0 = w[0], w1 = w[1], w2 = w[2];
   T qdd[3];
   qdd[2] = w2;
   qdd[1] = w1 - W.l21 * qdd[2];
