@@ -42,7 +42,7 @@ extern "C" {
 #define SPI_ENOMEM (-2)      /* device allocation failed */
 #define SPI_ECUDA (-3)       /* CUDA runtime error */
 #define SPI_ESTATE (-4)      /* call out of order (e.g. run before load) */
-#define SPI_ETIMEOUT (-5)    /* a bounded device wait ran out */
+#define SPI_ETIMEOUT (-5)    /* reserved: no entry point waits on the device (no kernel spins) */
 #define SPI_EBUDGET (-6)     /* request exceeds the admission budget */
 
 #define SPI_STATE_DIM 37     /* pos3 quat4(xyzw) linvel3 angvel3 (world) q12 qd12 */
@@ -151,7 +151,8 @@ int spi_read_costs(spi_engine* e, float* comp, float* cost);
 /* Copy the current theta batch [N][13] to theta (device or pinned host), async. */
 int spi_read_theta(spi_engine* e, float* theta);
 
-/* Wait for the engine stream; report rollouts whose final state was not finite. */
+/* Wait for the engine stream; report the number of (theta, window) rollouts whose final state
+ * was not finite, counted since spi_create. */
 int spi_sync(spi_engine* e, int64_t* n_nonfinite);
 
 /* ---- cross-entropy-method identification on the device -------------------------------

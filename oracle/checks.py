@@ -97,3 +97,22 @@ def momentum_world(x, theta, sim):
         ang = mv(R, hb[:, :3]) + np.cross(p, lin)
         h += np.concatenate([ang, lin], -1)
     return h
+
+
+def energy_world(x, theta, sim):
+    """Kinetic energy 1/2 sum_i v_i . (I_i v_i) plus gravitational potential energy
+    g sum_i m_i z_com,i of all bodies (contact and motor terms excluded)."""
+    from .dynamics import substep
+    _, aux = substep(x, np.zeros((x.shape[0], 12)), theta, sim, return_aux=True)
+    B = x.shape[0]
+    E = np.zeros(B)
+    I0 = np.broadcast_to(base_inertia(theta, sim), (B, 6, 6))
+    for i in range(gm.N_BODIES):
+        Ii = I0 if i == 0 else np.broadcast_to(_I_RIGID[i], (B, 6, 6))
+        v = aux["v"][i]
+        E += 0.5 * np.einsum("bk,bk->b", v, mv(Ii, v))
+        m = Ii[:, 3, 3]
+        h = np.stack([Ii[:, 2, 4], Ii[:, 0, 5], Ii[:, 1, 3]], -1)   # [h]x sits in the upper-right block
+        com = aux["pw"][i] + mv(aux["Rw"][i], h / m[:, None])
+        E += sim.gravity * m * com[:, 2]
+    return E
