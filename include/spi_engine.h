@@ -119,7 +119,8 @@ int spi_set_cost(spi_engine* e, int mode, const float* sq_weights);
  * other. */
 int spi_set_kernel_config(spi_engine* e, int min_blocks);
 
-/* Rollout-kernel lane layout. SPI_LAYOUT_QUAD: four lanes per rollout, one leg each, the base
+/* Rollout-kernel lane layout (default after spi_create: SPI_LAYOUT_LANE with min_blocks 3).
+ * SPI_LAYOUT_QUAD: four lanes per rollout, one leg each, the base
  * solved on all four. SPI_LAYOUT_LANE: one lane per rollout through all four legs, the model
  * in the kernel's parameter block, 66 KB of shared memory per 128-thread CTA (min_blocks 2 or
  * 3; min_blocks 4 keeps the last leg's work record in registers and needs 55 KB). Same equations, results within

@@ -135,6 +135,11 @@ int spi_create(const spi_robot* robot, spi_engine** out) {
   rc = e->bad.reserve(sizeof(unsigned long long));
   if (rc) { cudaFree(e->d_model); delete e; return rc; }
   cudaMemset(e->bad.p, 0, sizeof(unsigned long long));
+  // default kernel: the lane layout at 3 CTAs per SM (the fastest on the C1 workload)
+  if ((rc = spi_set_kernel_layout(e, SPI_LAYOUT_LANE)) || (rc = spi_set_kernel_config(e, 3))) {
+    spi_destroy(e);
+    return rc;
+  }
   *out = e;
   return SPI_OK;
 }
