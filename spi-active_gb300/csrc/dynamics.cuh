@@ -445,11 +445,14 @@ template <class T> struct LegWork {
   SV<T> Kp[3];
   T y[3];
   T l10, l20, l21;
-  // phase A hands its results over through these (a kernel may store them elsewhere, e.g.
-  // straight to shared memory, with a type that has the same members)
-  SPI_INL void put_K(int k, const SV<T>& v) { Kp[k] = v; }
-  SPI_INL void put_y(T y0, T y1, T y2) { y[0] = y0; y[1] = y1; y[2] = y2; }
-  SPI_INL void put_L(T a, T b, T c) { l10 = a; l20 = b; l21 = c; }
+  // phase A hands its results over through this, one joint column at a time: K'_k, y_k and
+  // the k-th factor entry (l10, l20, l21 in that order). A kernel may store them elsewhere,
+  // e.g. straight to shared memory, with a type that has the same member.
+  SPI_INL void put_col(int k, const SV<T>& v, T yk, T lk) {
+    Kp[k] = v;
+    y[k] = yk;
+    if (k == 0) l10 = lk; else if (k == 1) l20 = lk; else l21 = lk;
+  }
 };
 
 template <class T> SPI_INL M3<T> quat_to_R(T x, T y, T z, T w) {
@@ -662,9 +665,9 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
   const T z1 = (tau[1] - f1.w.y) - l10 * z0;
   const T z2 = (tau[2] - f2.w.y) - l20 * z0 - l21 * z1;
   const T y0 = z0 * i0, y1 = z1 * i1, y2 = z2 * i2;
-  W.put_K(0, Kp0); W.put_K(1, Kp1); W.put_K(2, Kp2);
-  W.put_y(y0, y1, y2);
-  W.put_L(l10, l20, l21);
+  W.put_col(0, Kp0, y0, l10);
+  W.put_col(1, Kp1, y1, l20);
+  W.put_col(2, Kp2, y2, l21);
   // the leg at the base: articulated inertia I_c - K D^-1 K^T, bias p_c + K y
   LegOut<T> out;
   out.I = ri_art(ri_to_parent<0, 7>(Rc0, C[0], S[0], r0));

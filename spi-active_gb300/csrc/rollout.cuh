@@ -66,36 +66,34 @@ __device__ __forceinline__ void load_model_smem(DevModel* dst, const DevModel* _
 // the [W][H][37] block of this theta.
 // The LegWork that phase C reads (24 floats: K'[3] 18, y 3, l10 / l20 / l21 3), parked in
 // shared memory between phase A and phase C so that its registers are free during the
-// reduction and the base solve. Field f of a thread lives at p[f * stride].
+// reduction and the base solve. It is six float4 fields, two per joint column k:
+// (K'_k.w, K'_k.v.x) and (K'_k.v.y, K'_k.v.z, y_k, l_k) with l = (l10, l20, l21); field f of a
+// thread lives at p[f * stride], so a warp's 128-bit accesses are conflict-free for stride 128.
 constexpr int kParkFloats = 24;
+constexpr int kParkVec = kParkFloats / 4;
 
-// Phase A's work record written straight to the parking area as each piece is produced, so
+// Phase A's work record written straight to the parking area as each column is produced, so
 // that none of it occupies registers for the rest of phase A.
 struct ParkedWork {
-  float* p;
+  float4* p;
   int stride;
-  __device__ __forceinline__ void put_K(int k, const SV<float>& v) {
-    float* q = p + 6 * k * stride;
-    q[0] = v.w.x; q[stride] = v.w.y; q[2 * stride] = v.w.z;
-    q[3 * stride] = v.v.x; q[4 * stride] = v.v.y; q[5 * stride] = v.v.z;
-  }
-  __device__ __forceinline__ void put_y(float y0, float y1, float y2) {
-    p[18 * stride] = y0; p[19 * stride] = y1; p[20 * stride] = y2;
-  }
-  __device__ __forceinline__ void put_L(float l10, float l20, float l21) {
-    p[21 * stride] = l10; p[22 * stride] = l20; p[23 * stride] = l21;
+  __device__ __forceinline__ void put_col(int k, const SV<float>& v, float yk, float lk) {
+    p[2 * k * stride] = make_float4(v.w.x, v.w.y, v.w.z, v.v.x);
+    p[(2 * k + 1) * stride] = make_float4(v.v.y, v.v.z, yk, lk);
   }
 };
 
-__device__ __forceinline__ void unpark_legwork(LegWork<float>& W, const float* src, int stride) {
+__device__ __forceinline__ void unpark_legwork(LegWork<float>& W, const float4* src, int stride) {
+  float l[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const float* q = src + 6 * k * stride;
-    W.Kp[k].w.x = q[0]; W.Kp[k].w.y = q[stride]; W.Kp[k].w.z = q[2 * stride];
-    W.Kp[k].v.x = q[3 * stride]; W.Kp[k].v.y = q[4 * stride]; W.Kp[k].v.z = q[5 * stride];
+    const float4 a = src[2 * k * stride], b = src[(2 * k + 1) * stride];
+    W.Kp[k].w = v3(a.x, a.y, a.z);
+    W.Kp[k].v = v3(a.w, b.x, b.y);
+    W.y[k] = b.z;
+    l[k] = b.w;
   }
-  W.y[0] = src[18 * stride]; W.y[1] = src[19 * stride]; W.y[2] = src[20 * stride];
-  W.l10 = src[21 * stride]; W.l20 = src[22 * stride]; W.l21 = src[23 * stride];
+  W.l10 = l[0]; W.l20 = l[1]; W.l21 = l[2];
 }
 
 // One physics substep of a lane quad: phase A (leg), quad reduction, phase B (base solve),
@@ -105,7 +103,7 @@ __device__ __forceinline__ void unpark_legwork(LegWork<float>& W, const float* s
 __device__ __forceinline__ void substep(const DevModel& M, int leg, BaseState<float>& B, LegState<float>& L,
                                         const BaseParams<float>& bp, const LegParams<float>& lp,
                                         const float act[3]) {
-  __shared__ float lw_smem[kParkFloats * 128];
+  __shared__ float4 lw_smem[kParkVec * 128];
   ParkedWork pw{lw_smem + threadIdx.x, 128};
   LegOut<float> o = phase_a(M, leg, B, L, lp, act, pw);
   qsum_out(o);

@@ -35,8 +35,8 @@ constexpr int kBaseFloats = 28;      // p 3, q 4 (xyzw), nu 6 (w, v), R 9, a0 6
 constexpr int kBaseParamFloats = 10; // m, h 3, Io 6
 
 struct BlockSmem {
+  float4 park[kParkVec * 128];
   float legout[kLegOutFloats * kLegOutStride];
-  float park[kParkFloats * 128];
   float base[kBaseFloats * 32];
   float bpar[kBaseParamFloats * 32];
 };

@@ -48,33 +48,69 @@ __device__ __forceinline__ float group8_sum(float x) {
 // model's per-leg constants are indexed loads from the kernel's parameter block. The
 // theta-derived base and leg parameters are one copy per warp (all lanes share theta).
 
-// Shared-memory layout per CTA, [field][128 threads] throughout: parking [P legs][kParkFloats],
-// then joint states [4 legs][6] (q 3, qd 3), then actions [12]. P = 4, or 3 when the last leg's
-// work record stays in registers (PEEL, for the 4-CTA-per-SM variant, whose 128-register cap
-// leaves room for it and whose shared-memory share is 55 KB).
-template <bool PEEL> __host__ __device__ constexpr int lane_leg_state() { return (PEEL ? 3 : 4) * kParkFloats * 128; }
-template <bool PEEL> __host__ __device__ constexpr int lane_act() { return lane_leg_state<PEEL>() + 4 * 6 * 128; }
-template <bool PEEL> __host__ __device__ constexpr int lane_smem_bytes() { return (lane_act<PEEL>() + 12 * 128) * (int)sizeof(float); }
+// Shared-memory layout per CTA: 16-byte fields, [field][128 threads] throughout, so that each
+// warp access is one conflict-free 128-bit load or store per field:
+//   parking      P legs x kParkVec fields (P = 4, or 3 when the last leg's work record stays in
+//                registers: PEEL, for the 4-CTA-per-SM variant, whose 128-register cap leaves
+//                room for it and whose shared-memory share is 54 KB);
+//   leg state a  4 legs x 1 field: (q0, q1, q2, qd0);
+//   actions      4 legs x 1 field: (a0, a1, a2, 0); with PEEL 3 fields, legs 0..2 in x, y, z and
+//                leg 3's three actions in their w;
+//   leg state b  4 legs x one 8-byte field: (qd1, qd2).
+// Offsets below are in 16-byte fields of 128 threads.
+template <bool PEEL> __host__ __device__ constexpr int lane_state_a() { return (PEEL ? 3 : 4) * kParkVec; }
+template <bool PEEL> __host__ __device__ constexpr int lane_act() { return lane_state_a<PEEL>() + 4; }
+template <bool PEEL> __host__ __device__ constexpr int lane_state_b() { return lane_act<PEEL>() + (PEEL ? 3 : 4); }
+template <bool PEEL> __host__ __device__ constexpr int lane_smem_bytes() {
+  return (lane_state_b<PEEL>() + 2) * 128 * (int)sizeof(float4);
+}
 constexpr int kLaneParkBytes = lane_smem_bytes<false>();
 constexpr int kLanePeelBytes = lane_smem_bytes<true>();
 
-__device__ __forceinline__ LegState<float> load_leg_state(const float* p) {
-  LegState<float> L;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) { L.q[k] = p[k * 128]; L.qd[k] = p[(3 + k) * 128]; }
-  return L;
-}
-__device__ __forceinline__ void store_leg_state(const LegState<float>& L, float* p) {
-#pragma unroll
-  for (int k = 0; k < 3; ++k) { p[k * 128] = L.q[k]; p[(3 + k) * 128] = L.qd[k]; }
-}
+// One thread's slots: sm = this thread's first 16-byte field; sb = its first (qd1, qd2) field.
+struct LaneSlots {
+  float4* sm;
+  float2* sb;
+  template <bool PEEL> __device__ __forceinline__ static LaneSlots of(float4* lane_smem) {
+    return LaneSlots{lane_smem + threadIdx.x,
+                     reinterpret_cast<float2*>(lane_smem + lane_state_b<PEEL>() * 128) + threadIdx.x};
+  }
+  template <bool PEEL> __device__ __forceinline__ LegState<float> leg_state(int leg) const {
+    const float4 u = sm[(lane_state_a<PEEL>() + leg) * 128];
+    const float2 v = sb[leg * 128];
+    LegState<float> L;
+    L.q[0] = u.x; L.q[1] = u.y; L.q[2] = u.z;
+    L.qd[0] = u.w; L.qd[1] = v.x; L.qd[2] = v.y;
+    return L;
+  }
+  template <bool PEEL> __device__ __forceinline__ void put_leg_state(int leg, const LegState<float>& L) const {
+    sm[(lane_state_a<PEEL>() + leg) * 128] = make_float4(L.q[0], L.q[1], L.q[2], L.qd[0]);
+    sb[leg * 128] = make_float2(L.qd[1], L.qd[2]);
+  }
+  __device__ __forceinline__ float4* park(int leg) const { return sm + leg * kParkVec * 128; }
+  // the twelve actions of one control step, legs in order
+  template <bool PEEL> __device__ __forceinline__ void put_actions(const float4 a0, const float4 a1,
+                                                                    const float4 a2) const {
+    float4* p = sm + lane_act<PEEL>() * 128;
+    if (PEEL) {
+      p[0] = make_float4(a0.x, a0.y, a0.z, a2.y);
+      p[128] = make_float4(a0.w, a1.x, a1.y, a2.z);
+      p[256] = make_float4(a1.z, a1.w, a2.x, a2.w);
+    } else {
+      p[0] = make_float4(a0.x, a0.y, a0.z, 0.f);
+      p[128] = make_float4(a0.w, a1.x, a1.y, 0.f);
+      p[256] = make_float4(a1.z, a1.w, a2.x, 0.f);
+      p[384] = make_float4(a2.y, a2.z, a2.w, 0.f);
+    }
+  }
+};
 
-// One physics substep of one rollout on one lane. sm: this thread's first shared-memory slot
-// (fields 128 floats apart); bp / lp: the warp's base and (front, rear) leg parameters.
+// One physics substep of one rollout on one lane. s: this thread's slots; bp / lp: the warp's
+// base and (front, rear) leg parameters.
 template <bool PEEL>
-__device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>& B, float* sm,
+__device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>& B, const LaneSlots& s,
                                              const BaseParams<float>* bp, const LegParams<float>* lp) {
-  constexpr int LS = lane_leg_state<PEEL>(), ACT = lane_act<PEEL>(), NP = PEEL ? 3 : 4;
+  constexpr int NP = PEEL ? 3 : 4;
   LegOut<float> sum;
   sum.I.A = S3<float>{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
   sum.I.C = sum.I.A;
@@ -84,37 +120,33 @@ __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>
     for (int j = 0; j < 3; ++j) sum.I.B.m[i][j] = 0.f;
   sum.p.w = v3(0.f, 0.f, 0.f);
   sum.p.v = sum.p.w;
+  const float4* act = s.sm + lane_act<PEEL>() * 128;
 #pragma unroll 1
   for (int leg = 0; leg < NP; ++leg) {
     const LegParams<float> P = lp[leg >> 1];
-    const float* ap = sm + ACT + 3 * leg * 128;
-    const float a3[3] = {ap[0], ap[128], ap[256]};
-    const LegState<float> L = load_leg_state(sm + LS + 6 * leg * 128);
-    ParkedWork pw{sm + leg * kParkFloats * 128, 128};
-    add_legout(sum, phase_a(M, leg, B, L, P, a3, pw));
+    const float4 a = act[leg * 128];
+    const float a3[3] = {a.x, a.y, a.z};
+    ParkedWork pw{s.park(leg), 128};
+    add_legout(sum, phase_a(M, leg, B, s.leg_state<PEEL>(leg), P, a3, pw));
   }
   LegWork<float> w3;
   if (PEEL) {
-    const float* ap = sm + ACT + 9 * 128;
-    const float a3[3] = {ap[0], ap[128], ap[256]};
-    const LegState<float> L = load_leg_state(sm + LS + 18 * 128);
-    add_legout(sum, phase_a(M, 3, B, L, lp[1], a3, w3));
+    const float a3[3] = {act[0].w, act[128].w, act[256].w};
+    add_legout(sum, phase_a(M, 3, B, s.leg_state<PEEL>(3), lp[1], a3, w3));
   }
   const SV<float> a0 = phase_b(M, *bp, sum, B);
   if (PEEL) {
-    float* ls = sm + LS + 18 * 128;
-    LegState<float> L = load_leg_state(ls);
+    LegState<float> L = s.leg_state<PEEL>(3);
     phase_c(M, 3, a0, w3, L);
-    store_leg_state(L, ls);
+    s.put_leg_state<PEEL>(3, L);
   }
 #pragma unroll 1
   for (int leg = 0; leg < NP; ++leg) {
-    float* ls = sm + LS + 6 * leg * 128;
-    LegState<float> L = load_leg_state(ls);
+    LegState<float> L = s.leg_state<PEEL>(leg);
     LegWork<float> lw;
-    unpark_legwork(lw, sm + leg * kParkFloats * 128, 128);
+    unpark_legwork(lw, s.park(leg), 128);
     phase_c(M, leg, a0, lw, L);
-    store_leg_state(L, ls);
+    s.put_leg_state<PEEL>(leg, L);
   }
 }
 
@@ -125,7 +157,7 @@ __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>
 template <bool PEEL>
 __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinView& win, const float* th13, int wb,
                                                   float* partial_n, int G, unsigned long long* n_bad,
-                                                  float* lane_smem, BaseParams<float>* bp_warp,
+                                                  float4* lane_smem, BaseParams<float>* bp_warp,
                                                   LegParams<float> (*lp_warp)[2]) {
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int W = win.W, H = win.H;
@@ -146,7 +178,7 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
     __syncwarp();
   }
 
-  float* my_sm = lane_smem + threadIdx.x;
+  const LaneSlots sl = LaneSlots::of<PEEL>(lane_smem);
   BaseState<float> B;
   {
     float s13[13];
@@ -161,24 +193,18 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
         L.q[k] = __ldg(win.init + (13 + 3 * leg + k) * W + w);
         L.qd[k] = __ldg(win.init + (25 + 3 * leg + k) * W + w);
       }
-      store_leg_state(L, my_sm + lane_leg_state<PEEL>() + 6 * leg * 128);
+      sl.put_leg_state<PEEL>(leg, L);
     }
   }
   const int dec = M.decimation;
   for (int h = 0; h < H; ++h) {
     const float4* ap = reinterpret_cast<const float4*>(win.act + ((size_t)h * W + w) * 12);
-    float* act = my_sm + lane_act<PEEL>();
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-      const float4 a = __ldg(ap + i);
-      act[(4 * i) * 128] = a.x; act[(4 * i + 1) * 128] = a.y;
-      act[(4 * i + 2) * 128] = a.z; act[(4 * i + 3) * 128] = a.w;
-    }
-    for (int s = 0; s < dec; ++s) substep_lane<PEEL>(M, B, my_sm, &bp_warp[wib], lp_warp[wib]);
+    sl.put_actions<PEEL>(__ldg(ap), __ldg(ap + 1), __ldg(ap + 2));
+    for (int s = 0; s < dec; ++s) substep_lane<PEEL>(M, B, sl, &bp_warp[wib], lp_warp[wib]);
   }
   LegState<float> L[4];
 #pragma unroll
-  for (int leg = 0; leg < 4; ++leg) L[leg] = load_leg_state(my_sm + lane_leg_state<PEEL>() + 6 * leg * 128);
+  for (int leg = 0; leg < 4; ++leg) L[leg] = sl.leg_state<PEEL>(leg);
   // final-step error components of this lane's window
   float s13[13];
   base_to_world(B, s13);
@@ -220,7 +246,7 @@ __global__ void __launch_bounds__(128, MINB) rollout_lane_kernel(const __grid_co
                                                                  const float* __restrict__ theta, int N, int G,
                                                                  float* __restrict__ partial,
                                                                  unsigned long long* __restrict__ n_bad) {
-  extern __shared__ float lane_smem[];               // lane_smem_bytes<(MINB >= 4)>()
+  extern __shared__ float4 lane_smem[];              // lane_smem_bytes<(MINB >= 4)>()
   __shared__ BaseParams<float> bp_warp[4];
   __shared__ LegParams<float> lp_warp[4][2];
   const int WB = (win.W + 31) >> 5;

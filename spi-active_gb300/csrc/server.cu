@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(128, MINB) server_rollout_lane_kernel(const __
                                                                   unsigned long long* __restrict__ counter_all,
                                                                   unsigned long long* __restrict__ n_bad,
                                                                   int max_slots, int round) {
-  extern __shared__ float lane_smem[];               // kLaneParkBytes
+  extern __shared__ float4 lane_smem[];              // kLaneParkBytes
   __shared__ BaseParams<float> bp_warp[4];
   __shared__ LegParams<float> lp_warp[4][2];
   const int lane = threadIdx.x & 31;
