@@ -247,6 +247,14 @@ template <int AX, class T> SPI_INL SV<T> ri_col(const RI<T>& a) {
 }
 // Articulated-inertia form [[I, [h]x], [[h]x^T, m 1]].
 template <class T> SPI_INL Art<T> ri_art(const RI<T>& a) { return rigid(a.m, a.h, a.I); }
+// I += ri_art(a), its structural zeros not added.
+template <class T> SPI_INL void ri_art_add(Art<T>& I, const RI<T>& a) {
+  I.A.xx += a.I.xx; I.A.yy += a.I.yy; I.A.zz += a.I.zz; I.A.xy += a.I.xy; I.A.xz += a.I.xz; I.A.yz += a.I.yz;
+  I.B.m[0][1] -= a.h.z; I.B.m[0][2] += a.h.y;
+  I.B.m[1][0] += a.h.z; I.B.m[1][2] -= a.h.x;
+  I.B.m[2][0] -= a.h.y; I.B.m[2][1] += a.h.x;
+  I.C.xx += a.m; I.C.yy += a.m; I.C.zz += a.m;
+}
 
 // Joint-origin sparsity. RM = 2: origin on the y axis (thigh joints), RM = 4: on the z axis
 // (calf joints), RM = 7: general (hip joints). The model builder checks the pattern.
@@ -583,9 +591,11 @@ template <class T> SPI_INL void art_sub_outer(Art<T>& I, const SV<T>& a, const S
 // base, I_c - F M^-1 F^T and p_c + F M^-1 (tau - C) -- the quantities Featherstone's ABA
 // backward pass produces, from fewer operations for a three-joint chain.
 // ---------------------------------------------------------------------------
-template <class T, class WK>
-SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
-                          const LegParams<T>& P, const T act[3], WK& W) {
+// ACC = false: out receives the leg's contribution; ACC = true: the contribution is added to out
+// (the running sum over legs, which may start from the base body's own terms).
+template <bool ACC, class T, class WK>
+SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
+                          const LegParams<T>& P, const T act[3], WK& W, LegOut<T>& out) {
   T tau[3], C[3], S[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -641,7 +651,7 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
     const RI<T> Ihp = leg_ri<T>(M, 0, leg);
     f0 = ri_mul_acc(Ihp, cb0, crf_acc(v0, ri_mul(Ihp, v0), force_to_parent<1, 2>(f1, C[1], S[1], r1)));
   }
-  const SV<T> pc = force_to_parent<0, 7>(f0, C[0], S[0], r0);
+  const SV<T> pc = ACC ? force_to_parent_acc<0, 7>(f0, C[0], S[0], r0, out.p) : force_to_parent<0, 7>(f0, C[0], S[0], r0);
   // joint force columns F_k = I_k^c S_k in base coordinates, and the joint-space inertia
   const SV<T> F2t = force_to_parent<1, 4>(ri_col<1>(Rc2), C[2], S[2], r2);
   const SV<T> F2h = force_to_parent<1, 2>(F2t, C[1], S[1], r1);
@@ -669,8 +679,8 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
   W.put_col(1, Kp1, y1, l20);
   W.put_col(2, Kp2, y2, l21);
   // the leg at the base: articulated inertia I_c - K D^-1 K^T, bias p_c + K y
-  LegOut<T> out;
-  out.I = ri_art(ri_to_parent<0, 7>(Rc0, C[0], S[0], r0));
+  if (ACC) ri_art_add(out.I, ri_to_parent<0, 7>(Rc0, C[0], S[0], r0));
+  else out.I = ri_art(ri_to_parent<0, 7>(Rc0, C[0], S[0], r0));
   art_sub_outer(out.I, Kp0, K0);
   art_sub_outer(out.I, Kp1, K1);
   art_sub_outer(out.I, Kp2, K2);
@@ -697,7 +707,20 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
       add_point_mass(out.I, mc, rc);
     }
   }
+}
+
+template <class T, class WK>
+SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
+                          const LegParams<T>& P, const T act[3], WK& W) {
+  LegOut<T> out;
+  phase_a_core<false>(M, leg, B, L, P, act, W, out);
   return out;
+}
+// Phase A adding the leg's contribution to acc.
+template <class T, class WK>
+SPI_INL void phase_a_into(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
+                          const LegParams<T>& P, const T act[3], WK& W, LegOut<T>& acc) {
+  phase_a_core<true>(M, leg, B, L, P, act, W, acc);
 }
 
 // ---------------------------------------------------------------------------
@@ -705,10 +728,28 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
 // Returns the base acceleration with gravity removed (the frame the legs' forward pass uses).
 // ---------------------------------------------------------------------------
 template <class T>
+SPI_INL SV<T> base_solve(const DevModel& M, const Art<T>& IA, const SV<T>& pA, BaseState<T>& B);
+
+template <class T>
 SPI_INL SV<T> phase_b(const DevModel& M, const BaseParams<T>& bp, const LegOut<T>& sum, BaseState<T>& B) {
   Art<T> IA = rigid(bp.m, bp.h, bp.Io);
   add_to(IA, sum.I);
-  const SV<T> pA = crf_acc(B.nu, rigid_mul(bp.m, bp.h, bp.Io, B.nu), sum.p);
+  return base_solve(M, IA, crf_acc(B.nu, rigid_mul(bp.m, bp.h, bp.Io, B.nu), sum.p), B);
+}
+
+// The base body's own terms, the start of a running sum over legs (phase_a_into) that
+// base_solve then takes as the total articulated inertia and bias force.
+template <class T> SPI_INL LegOut<T> base_terms(const BaseParams<T>& bp, const BaseState<T>& B) {
+  LegOut<T> o;
+  o.I = rigid(bp.m, bp.h, bp.Io);
+  o.p = crf(B.nu, rigid_mul(bp.m, bp.h, bp.Io, B.nu));
+  return o;
+}
+
+// Base solve and base integration from the total articulated inertia IA and bias force pA at
+// the base. Returns the base acceleration with gravity removed.
+template <class T>
+SPI_INL SV<T> base_solve(const DevModel& M, const Art<T>& IA, const SV<T>& pA, BaseState<T>& B) {
   // 6x6 symmetric matrix in (w; v) order, Cholesky L L^T, solve IA a = -pA
   T Mx[6][6];
   Mx[0][0] = IA.A.xx; Mx[1][1] = IA.A.yy; Mx[2][2] = IA.A.zz;

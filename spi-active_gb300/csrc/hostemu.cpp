@@ -55,14 +55,20 @@ static void substep(const DevModel& M, BaseState<T>& B, LegState<T> L[4], const 
                     const LegParams<T> lp[4], const T act[12]) {
   LegWork<T> W[4];
   aba::AbaWork<T> Wa[4];
-  LegOut<T> o[4];
-  for (int leg = 0; leg < 4; ++leg)
-    o[leg] = ABA ? aba::phase_a_aba(M, leg, B, L[leg], lp[leg], act + 3 * leg, Wa[leg])
-                 : phase_a(M, leg, B, L[leg], lp[leg], act + 3 * leg, W[leg]);
-  add_out(o[0], o[1]);
-  add_out(o[2], o[3]);
-  add_out(o[0], o[2]);
-  SV<T> a0 = phase_b(M, bp, o[0], B);
+  SV<T> a0;
+  if (ABA) {
+    LegOut<T> o[4];
+    for (int leg = 0; leg < 4; ++leg) o[leg] = aba::phase_a_aba(M, leg, B, L[leg], lp[leg], act + 3 * leg, Wa[leg]);
+    add_out(o[0], o[1]);
+    add_out(o[2], o[3]);
+    add_out(o[0], o[2]);
+    a0 = phase_b(M, bp, o[0], B);
+  } else {
+    // as the lane-per-rollout kernel: the legs summed onto the base body's own terms in order
+    LegOut<T> sum = base_terms(bp, B);
+    for (int leg = 0; leg < 4; ++leg) phase_a_into(M, leg, B, L[leg], lp[leg], act + 3 * leg, W[leg], sum);
+    a0 = base_solve(M, sum.I, sum.p, B);
+  }
   for (int leg = 0; leg < 4; ++leg) {
     if (ABA) aba::phase_c_aba(M, leg, a0, Wa[leg], L[leg]);
     else phase_c(M, leg, a0, W[leg], L[leg]);
@@ -190,15 +196,12 @@ int spi_hostemu_count_phases(const spi_robot* robot, const double* state, const 
   Cf act[12];
   for (int j = 0; j < 12; ++j) act[j] = Cf(act12[j]);
   LegWork<Cf> W[4];
-  LegOut<Cf> o[4];
   Cf::n = 0;
-  for (int leg = 0; leg < 4; ++leg) o[leg] = phase_a(M, leg, B, L[leg], lp[leg], act + 3 * leg, W[leg]);
-  add_out(o[0], o[1]);
-  add_out(o[2], o[3]);
-  add_out(o[0], o[2]);
+  LegOut<Cf> sum = base_terms(bp, B);
+  for (int leg = 0; leg < 4; ++leg) phase_a_into(M, leg, B, L[leg], lp[leg], act + 3 * leg, W[leg], sum);
   out3[0] = Cf::n;
   Cf::n = 0;
-  SV<Cf> a0 = phase_b(M, bp, o[0], B);
+  SV<Cf> a0 = base_solve(M, sum.I, sum.p, B);
   out3[1] = Cf::n;
   Cf::n = 0;
   for (int leg = 0; leg < 4; ++leg) phase_c(M, leg, a0, W[leg], L[leg]);

@@ -21,19 +21,6 @@
 
 namespace spi {
 
-__device__ __forceinline__ void add_legout(LegOut<float>& a, const LegOut<float>& b) {
-  a.I.A.xx += b.I.A.xx; a.I.A.yy += b.I.A.yy; a.I.A.zz += b.I.A.zz;
-  a.I.A.xy += b.I.A.xy; a.I.A.xz += b.I.A.xz; a.I.A.yz += b.I.A.yz;
-  a.I.C.xx += b.I.C.xx; a.I.C.yy += b.I.C.yy; a.I.C.zz += b.I.C.zz;
-  a.I.C.xy += b.I.C.xy; a.I.C.xz += b.I.C.xz; a.I.C.yz += b.I.C.yz;
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) a.I.B.m[i][j] += b.I.B.m[i][j];
-  a.p.w = a.p.w + b.p.w;
-  a.p.v = a.p.v + b.p.v;
-}
-
 // Sum over the eight lanes of a window group (lanes with equal lane >> 3).
 __device__ __forceinline__ float group8_sum(float x) {
   x += __shfl_xor_sync(0xffffffffu, x, 1);
@@ -111,15 +98,8 @@ template <bool PEEL>
 __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>& B, const LaneSlots& s,
                                              const BaseParams<float>* bp, const LegParams<float>* lp) {
   constexpr int NP = PEEL ? 3 : 4;
-  LegOut<float> sum;
-  sum.I.A = S3<float>{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  sum.I.C = sum.I.A;
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) sum.I.B.m[i][j] = 0.f;
-  sum.p.w = v3(0.f, 0.f, 0.f);
-  sum.p.v = sum.p.w;
+  // articulated inertia and bias force at the base: the base body's own, plus each leg's
+  LegOut<float> sum = base_terms(*bp, B);
   const float4* act = s.sm + lane_act<PEEL>() * 128;
 #pragma unroll 1
   for (int leg = 0; leg < NP; ++leg) {
@@ -127,14 +107,14 @@ __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>
     const float4 a = act[leg * 128];
     const float a3[3] = {a.x, a.y, a.z};
     ParkedWork pw{s.park(leg), 128};
-    add_legout(sum, phase_a(M, leg, B, s.leg_state<PEEL>(leg), P, a3, pw));
+    phase_a_into(M, leg, B, s.leg_state<PEEL>(leg), P, a3, pw, sum);
   }
   LegWork<float> w3;
   if (PEEL) {
     const float a3[3] = {act[0].w, act[128].w, act[256].w};
-    add_legout(sum, phase_a(M, 3, B, s.leg_state<PEEL>(3), lp[1], a3, w3));
+    phase_a_into(M, 3, B, s.leg_state<PEEL>(3), lp[1], a3, w3, sum);
   }
-  const SV<float> a0 = phase_b(M, *bp, sum, B);
+  const SV<float> a0 = base_solve(M, sum.I, sum.p, B);
   if (PEEL) {
     LegState<float> L = s.leg_state<PEEL>(3);
     phase_c(M, 3, a0, w3, L);

@@ -18,7 +18,7 @@ from helpers import random_theta
 # the ground): the articulated-body formulation of the oracle (csrc/aba_reference.h), the
 # roofline's algorithmic figure, and the kernel's condensed formulation (csrc/dynamics.cuh).
 FLOPS_PER_SUBSTEP = 7053
-EXECUTED_FLOPS_PER_SUBSTEP = 5961
+EXECUTED_FLOPS_PER_SUBSTEP = 5937
 
 
 def _emu(built, cfg, x0, acts, th):
