@@ -48,17 +48,40 @@ namespace spi {
 // ---------------------------------------------------------------------------
 SPI_INL float m_sqrt(float x) { return sqrtf(x); }
 SPI_INL double m_sqrt(double x) { return sqrt(x); }
-// Device FP32: tanh from one MUFU exponential, 1 - 2/(e^{2x} + 1) (absolute error ~1e-7; the
-// exponent is clamped so e^{2x} stays finite).
+// Device FP32: tanh(x) = 1 - 2/(2^{x k} + 1) with k = 2 log2(e), from one MUFU base-2
+// exponential and one MUFU reciprocal (absolute error ~1e-7). Large |x| needs no clamp: the
+// exponential saturates to +inf or 0 and the expression to +1 or -1; NaN propagates.
+constexpr float kTwoLog2e = 2.88539008177792681f;
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float tanh_from_k(float xk) { return 1.0f - __fdividef(2.0f, ex2_approx(xk) + 1.0f); }
+#endif
 SPI_INL float m_tanh(float x) {
 #if defined(__CUDA_ARCH__)
-  const float e = __expf(2.0f * fminf(fmaxf(x, -15.0f), 15.0f));
-  return 1.0f - __fdividef(2.0f, e + 1.0f);
+  return tanh_from_k(x * kTwoLog2e);
 #else
   return tanhf(x);
 #endif
 }
 SPI_INL double m_tanh(double x) { return tanh(x); }
+// tanh(x / d) given k2 = 2 log2(e) / d and x / d given dinv = 1 / d (model constants): the FP32
+// forms multiply by the precomputed constant, every other scalar type divides.
+SPI_INL float m_tanh_div(float x, float d, float k2) {
+#if defined(__CUDA_ARCH__)
+  (void)d;
+  return tanh_from_k(x * k2);
+#else
+  (void)k2;
+  return tanhf(x / d);
+#endif
+}
+template <class T> SPI_INL T m_tanh_div(T x, float d, float k2) { (void)k2; return m_tanh(x / T(d)); }
+SPI_INL float m_div_c(float x, float d, float dinv) { (void)d; return x * dinv; }
+template <class T> SPI_INL T m_div_c(T x, float d, float dinv) { (void)dinv; return x / T(d); }
 // Device FP32: reduce to [-pi, pi] (joint angles stay within a few radians), then the MUFU
 // sine / cosine, whose absolute error there is ~2^-21.
 SPI_INL void m_sincos(float x, float* s, float* c) {
@@ -420,6 +443,7 @@ struct DevModel {
   float h[3][3][4];
   float I[3][6][4];   // xx yy zz xy xz yz about the body origin
   float kp[3][4], kd[3][4], q0[3][4], tlim[3][4], vlim[3][4];
+  float vlim_inv[3][4];   // 1 / vlim (0 without the torque-speed limit)
   float corner[8][3];
   float foot[3];
   float gain[3], tanh_a[3];
@@ -428,6 +452,7 @@ struct DevModel {
   float foot_r, k, c, ct, mu, ramp_inv, imp_c;
   float corner_reach;   // largest distance of a base-box corner from the base origin
   float kd_scale, act_scale, act_clip, hip_scale, fric_vel;
+  float fric_k2;          // 2 log2(e) / fric_vel
   float dt, g;
   int decimation, torque_speed, base_contact, inertia_follows_mass;
 };
@@ -525,16 +550,25 @@ template <class T> SPI_INL void add_point_mass(Art<T>& I, T m, V3<T> r) {
   I.C.xx += m; I.C.yy += m; I.C.zz += m;
 }
 
-template <class T> SPI_INL T motor_torque(const DevModel& M, const LegParams<T>& P, int k, int leg,
-                                          T action, T q, T qd) {
+// Joint k's position target for an action (constant over a control step's substeps).
+template <class T> SPI_INL T joint_target(const DevModel& M, int k, int leg, T action) {
   T a = m_clamp(action, T(-M.act_clip), T(M.act_clip)) * T(M.act_scale);
   if (k == 0) a = a * T(M.hip_scale);
-  T tau = P.kps * T(M.kp[k][leg]) * (a + T(M.q0[k][leg]) - q) - T(M.kd_scale) * T(M.kd[k][leg]) * qd;
+  return a + T(M.q0[k][leg]);
+}
+// Motor torque of joint k towards its position target.
+template <class T> SPI_INL T motor_torque_at(const DevModel& M, const LegParams<T>& P, int k, int leg,
+                                             T target, T q, T qd) {
+  T tau = P.kps * T(M.kp[k][leg]) * (target - q) - T(M.kd_scale) * T(M.kd[k][leg]) * qd;
   T lim = P.ts * T(M.tlim[k][leg]);
-  if (M.torque_speed) lim = lim * m_fmax(T(0), T(1) - m_fabs(qd) / T(M.vlim[k][leg]));
+  if (M.torque_speed) lim = lim * m_fmax(T(0), T(1) - m_div_c(m_fabs(qd), M.vlim[k][leg], M.vlim_inv[k][leg]));
   tau = m_clamp(tau, -lim, lim) * T(M.gain[k]);
   if (M.tanh_a[k] > 0.0f) tau = T(M.tanh_a[k]) * m_tanh(tau / T(M.tanh_a[k]));
-  return tau - P.fc * m_tanh(qd / T(M.fric_vel));
+  return tau - P.fc * m_tanh_div(qd, M.fric_vel, M.fric_k2);
+}
+template <class T> SPI_INL T motor_torque(const DevModel& M, const LegParams<T>& P, int k, int leg,
+                                          T action, T q, T qd) {
+  return motor_torque_at(M, P, k, leg, joint_target(M, k, leg, action), q, qd);
 }
 
 template <class T> SPI_INL V3<T> leg_org(const DevModel& M, int k, int leg) {
@@ -593,13 +627,14 @@ template <class T> SPI_INL void art_sub_outer(Art<T>& I, const SV<T>& a, const S
 // ---------------------------------------------------------------------------
 // ACC = false: out receives the leg's contribution; ACC = true: the contribution is added to out
 // (the running sum over legs, which may start from the base body's own terms).
-template <bool ACC, class T, class WK>
+// TGT = false: act holds the leg's three actions; TGT = true: their joint targets (joint_target).
+template <bool ACC, bool TGT, class T, class WK>
 SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
                           const LegParams<T>& P, const T act[3], WK& W, LegOut<T>& out) {
   T tau[3], C[3], S[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    tau[k] = motor_torque(M, P, k, leg, act[k], L.q[k], L.qd[k]);
+    tau[k] = motor_torque_at(M, P, k, leg, TGT ? act[k] : joint_target(M, k, leg, act[k]), L.q[k], L.qd[k]);
     m_sincos(L.q[k], &S[k], &C[k]);
   }
   V3<T> r0 = leg_org<T>(M, 0, leg), r1 = leg_org<T>(M, 1, leg), r2 = leg_org<T>(M, 2, leg);
@@ -713,14 +748,15 @@ template <class T, class WK>
 SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
                           const LegParams<T>& P, const T act[3], WK& W) {
   LegOut<T> out;
-  phase_a_core<false>(M, leg, B, L, P, act, W, out);
+  phase_a_core<false, false>(M, leg, B, L, P, act, W, out);
   return out;
 }
-// Phase A adding the leg's contribution to acc.
+// Phase A adding the leg's contribution to acc, from the leg's joint targets tgt (joint_target
+// of its three actions, formed once per control step).
 template <class T, class WK>
 SPI_INL void phase_a_into(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
-                          const LegParams<T>& P, const T act[3], WK& W, LegOut<T>& acc) {
-  phase_a_core<true>(M, leg, B, L, P, act, W, acc);
+                          const LegParams<T>& P, const T tgt[3], WK& W, LegOut<T>& acc) {
+  phase_a_core<true, true>(M, leg, B, L, P, tgt, W, acc);
 }
 
 // ---------------------------------------------------------------------------

@@ -49,7 +49,8 @@ template <class T> static void add_out(LegOut<T>& a, const LegOut<T>& b) {
   a.p.v = a.p.v + b.p.v;
 }
 
-// ABA = false: the kernel's condensed legs; true: the oracle's articulated-body algorithm.
+// ABA = false: the kernel's condensed legs, act = the twelve joint targets (joint_target);
+// true: the oracle's articulated-body algorithm, act = the twelve actions.
 template <bool ABA, class T>
 static void substep(const DevModel& M, BaseState<T>& B, LegState<T> L[4], const BaseParams<T>& bp,
                     const LegParams<T> lp[4], const T act[12]) {
@@ -112,7 +113,7 @@ static int hostemu_rollout(const spi_robot* robot, const double* init, const dou
     for (int h = 0; h < H; ++h) {
       const double* a = actions + ((size_t)b * H + h) * 12;
       T act[12];
-      for (int j = 0; j < 12; ++j) act[j] = T(a[j]);
+      for (int j = 0; j < 12; ++j) act[j] = ABA ? T(a[j]) : joint_target(M, j % 3, j / 3, T(a[j]));
       for (int s = 0; s < M.decimation; ++s) substep<ABA>(M, B, L, bp, lp, act);
       double* out = trace + ((size_t)b * H + h) * SPI_STATE_DIM;
       T s13[13];
@@ -142,8 +143,9 @@ static int count_ops(const spi_robot* robot, const double* state, const double* 
   Cf::n = 0;
   load_rollout(M, state, theta, B, L, bp, lp);
   if (per_rollout_setup) *per_rollout_setup = Cf::n;
+  // the joint targets are formed once per control step, outside the substep counted here
   Cf act[12];
-  for (int j = 0; j < 12; ++j) act[j] = Cf(act12[j]);
+  for (int j = 0; j < 12; ++j) act[j] = ABA ? Cf(act12[j]) : joint_target(M, j % 3, j / 3, Cf(act12[j]));
   Cf::n = 0;
   substep<ABA>(M, B, L, bp, lp, act);
   if (per_substep) *per_substep = Cf::n;
@@ -194,7 +196,7 @@ int spi_hostemu_count_phases(const spi_robot* robot, const double* state, const 
   LegParams<Cf> lp[4];
   load_rollout(M, state, theta, B, L, bp, lp);
   Cf act[12];
-  for (int j = 0; j < 12; ++j) act[j] = Cf(act12[j]);
+  for (int j = 0; j < 12; ++j) act[j] = joint_target(M, j % 3, j / 3, Cf(act12[j]));
   LegWork<Cf> W[4];
   Cf::n = 0;
   LegOut<Cf> sum = base_terms(bp, B);

@@ -26,6 +26,7 @@ inline int build_dev_model(const spi_robot& r, DevModel* M, const char** why) {
       M->q0[k][leg] = r.default_q[b];
       M->tlim[k][leg] = r.torque_limit[b];
       M->vlim[k][leg] = r.velocity_limit[b];
+      M->vlim_inv[k][leg] = r.torque_speed ? (float)(1.0 / (double)r.velocity_limit[b]) : 0.0f;
       if (!(r.body_mass[b] > 0.0f)) { *why = "leg body mass must be > 0"; return SPI_EINVAL; }
       // the kernel's transforms assume thigh joints offset along y and calf joints along z
       if (k == 1 && (r.body_origin[b][0] != 0.0f || r.body_origin[b][2] != 0.0f)) {
@@ -70,6 +71,7 @@ inline int build_dev_model(const spi_robot& r, DevModel* M, const char** why) {
     *why = "sim_dt must be > 0 and decimation in [1, 64]"; return SPI_EINVAL;
   }
   if (!(r.friction_vel > 0.0f)) { *why = "friction_vel must be > 0"; return SPI_EINVAL; }
+  M->fric_k2 = (float)(2.0 / (log(2.0) * (double)r.friction_vel));
   if (r.inertia_follows_mass && !(r.base_mass_nominal > 0.0f)) {
     *why = "base_mass_nominal must be > 0 with inertia_follows_mass"; return SPI_EINVAL;
   }

@@ -41,8 +41,8 @@ __device__ __forceinline__ float group8_sum(float x) {
 //                registers: PEEL, for the 4-CTA-per-SM variant, whose 128-register cap leaves
 //                room for it and whose shared-memory share is 54 KB);
 //   leg state a  4 legs x 1 field: (q0, q1, q2, qd0);
-//   actions      4 legs x 1 field: (a0, a1, a2, 0); with PEEL 3 fields, legs 0..2 in x, y, z and
-//                leg 3's three actions in their w;
+//   targets      4 legs x 1 field: the joint targets of the control step's actions (t0, t1, t2, 0);
+//                with PEEL 3 fields, legs 0..2 in x, y, z and leg 3's three targets in their w;
 //   leg state b  4 legs x one 8-byte field: (qd1, qd2).
 // Offsets below are in 16-byte fields of 128 threads.
 template <bool PEEL> __host__ __device__ constexpr int lane_state_a() { return (PEEL ? 3 : 4) * kParkVec; }
@@ -75,19 +75,23 @@ struct LaneSlots {
     sb[leg * 128] = make_float2(L.qd[1], L.qd[2]);
   }
   __device__ __forceinline__ float4* park(int leg) const { return sm + leg * kParkVec * 128; }
-  // the twelve actions of one control step, legs in order
-  template <bool PEEL> __device__ __forceinline__ void put_actions(const float4 a0, const float4 a1,
-                                                                    const float4 a2) const {
+  // the joint targets of the twelve actions of one control step (legs in order)
+  template <bool PEEL> __device__ __forceinline__ void put_targets(const DevModel& M, const float4 a0,
+                                                                    const float4 a1, const float4 a2) const {
+    const float a[12] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w, a2.x, a2.y, a2.z, a2.w};
+    float t[12];
+#pragma unroll
+    for (int j = 0; j < 12; ++j) t[j] = joint_target(M, j % 3, j / 3, a[j]);
     float4* p = sm + lane_act<PEEL>() * 128;
     if (PEEL) {
-      p[0] = make_float4(a0.x, a0.y, a0.z, a2.y);
-      p[128] = make_float4(a0.w, a1.x, a1.y, a2.z);
-      p[256] = make_float4(a1.z, a1.w, a2.x, a2.w);
+      p[0] = make_float4(t[0], t[1], t[2], t[9]);
+      p[128] = make_float4(t[3], t[4], t[5], t[10]);
+      p[256] = make_float4(t[6], t[7], t[8], t[11]);
     } else {
-      p[0] = make_float4(a0.x, a0.y, a0.z, 0.f);
-      p[128] = make_float4(a0.w, a1.x, a1.y, 0.f);
-      p[256] = make_float4(a1.z, a1.w, a2.x, 0.f);
-      p[384] = make_float4(a2.y, a2.z, a2.w, 0.f);
+      p[0] = make_float4(t[0], t[1], t[2], 0.f);
+      p[128] = make_float4(t[3], t[4], t[5], 0.f);
+      p[256] = make_float4(t[6], t[7], t[8], 0.f);
+      p[384] = make_float4(t[9], t[10], t[11], 0.f);
     }
   }
 };
@@ -100,18 +104,18 @@ __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>
   constexpr int NP = PEEL ? 3 : 4;
   // articulated inertia and bias force at the base: the base body's own, plus each leg's
   LegOut<float> sum = base_terms(*bp, B);
-  const float4* act = s.sm + lane_act<PEEL>() * 128;
+  const float4* tgt = s.sm + lane_act<PEEL>() * 128;
 #pragma unroll 1
   for (int leg = 0; leg < NP; ++leg) {
     const LegParams<float> P = lp[leg >> 1];
-    const float4 a = act[leg * 128];
+    const float4 a = tgt[leg * 128];
     const float a3[3] = {a.x, a.y, a.z};
     ParkedWork pw{s.park(leg), 128};
     phase_a_into(M, leg, B, s.leg_state<PEEL>(leg), P, a3, pw, sum);
   }
   LegWork<float> w3;
   if (PEEL) {
-    const float a3[3] = {act[0].w, act[128].w, act[256].w};
+    const float a3[3] = {tgt[0].w, tgt[128].w, tgt[256].w};
     phase_a_into(M, 3, B, s.leg_state<PEEL>(3), lp[1], a3, w3, sum);
   }
   const SV<float> a0 = base_solve(M, sum.I, sum.p, B);
@@ -179,7 +183,7 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
   const int dec = M.decimation;
   for (int h = 0; h < H; ++h) {
     const float4* ap = reinterpret_cast<const float4*>(win.act + ((size_t)h * W + w) * 12);
-    sl.put_actions<PEEL>(__ldg(ap), __ldg(ap + 1), __ldg(ap + 2));
+    sl.put_targets<PEEL>(M, __ldg(ap), __ldg(ap + 1), __ldg(ap + 2));
     for (int s = 0; s < dec; ++s) substep_lane<PEEL>(M, B, sl, &bp_warp[wib], lp_warp[wib]);
   }
   LegState<float> L[4];

@@ -16,9 +16,10 @@ from helpers import random_theta
 
 # Instrumented counts at the default configuration and a standing state (base-box corners off
 # the ground): the articulated-body formulation of the oracle (csrc/aba_reference.h), the
-# roofline's algorithmic figure, and the kernel's condensed formulation (csrc/dynamics.cuh).
+# roofline's algorithmic figure, and the kernel's condensed formulation (csrc/dynamics.cuh; the
+# joint targets of the actions are formed once per control step, outside the substep).
 FLOPS_PER_SUBSTEP = 7053
-EXECUTED_FLOPS_PER_SUBSTEP = 5937
+EXECUTED_FLOPS_PER_SUBSTEP = 5909
 
 
 def _emu(built, cfg, x0, acts, th):
