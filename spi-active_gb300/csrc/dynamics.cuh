@@ -82,6 +82,10 @@ SPI_INL float m_tanh_div(float x, float d, float k2) {
 template <class T> SPI_INL T m_tanh_div(T x, float d, float k2) { (void)k2; return m_tanh(x / T(d)); }
 SPI_INL float m_div_c(float x, float d, float dinv) { (void)d; return x * dinv; }
 template <class T> SPI_INL T m_div_c(T x, float d, float dinv) { (void)dinv; return x / T(d); }
+// a b x given ab = fl(a b) (a model constant): FP32 multiplies once, to the same result as
+// (a b) x; every other scalar type forms a b in its own precision.
+SPI_INL float m_mul2_c(float x, float a, float b, float ab) { (void)a; (void)b; return ab * x; }
+template <class T> SPI_INL T m_mul2_c(T x, float a, float b, float ab) { (void)ab; return T(a) * T(b) * x; }
 // Device FP32: reduce to [-pi, pi] (joint angles stay within a few radians), then the MUFU
 // sine / cosine, whose absolute error there is ~2^-21.
 SPI_INL void m_sincos(float x, float* s, float* c) {
@@ -291,12 +295,12 @@ template <int RM, class T> SPI_INL V3<T> rcross(V3<T> r, V3<T> u) {
 template <int RM, class T> SPI_INL V3<T> sub_rcross(V3<T> u, V3<T> r, V3<T> w) {
   if (RM == 2) return v3(u.x - r.y * w.z, u.y, u.z + r.y * w.x);
   if (RM == 4) return v3(u.x + r.z * w.y, u.y - r.z * w.x, u.z);
-  return u - cross(r, w);
+  return v3(u.x - r.y * w.z + r.z * w.y, u.y - r.z * w.x + r.x * w.z, u.z - r.x * w.y + r.y * w.x);
 }
 template <int RM, class T> SPI_INL V3<T> add_rcross(V3<T> u, V3<T> r, V3<T> w) {
   if (RM == 2) return v3(u.x + r.y * w.z, u.y, u.z - r.y * w.x);
   if (RM == 4) return v3(u.x - r.z * w.y, u.y + r.z * w.x, u.z);
-  return u + cross(r, w);
+  return v3(u.x + r.y * w.z - r.z * w.y, u.y + r.z * w.x - r.x * w.z, u.z + r.x * w.y - r.y * w.x);
 }
 // acc + R u for the active rotation about AX.
 template <int AX, class T> SPI_INL V3<T> rot_acc(T c, T s, V3<T> u, V3<T> acc) {
@@ -444,6 +448,7 @@ struct DevModel {
   float I[3][6][4];   // xx yy zz xy xz yz about the body origin
   float kp[3][4], kd[3][4], q0[3][4], tlim[3][4], vlim[3][4];
   float vlim_inv[3][4];   // 1 / vlim (0 without the torque-speed limit)
+  float kdd[3][4];        // kd_scale kd (float product)
   float corner[8][3];
   float foot[3];
   float gain[3], tanh_a[3];
@@ -453,6 +458,7 @@ struct DevModel {
   float corner_reach;   // largest distance of a base-box corner from the base origin
   float kd_scale, act_scale, act_clip, hip_scale, fric_vel;
   float fric_k2;          // 2 log2(e) / fric_vel
+  float dt_imp_c;         // dt imp_c (float product)
   float dt, g;
   int decimation, torque_speed, base_contact, inertia_follows_mass;
 };
@@ -535,7 +541,7 @@ template <class T> SPI_INL V3<T> contact_force(const DevModel& M, T radius, T z,
   T vtn = m_sqrt(v.x * v.x + v.y * v.y);
   T lim = T(M.mu) * fn;
   T scale = m_sel(T(M.ct) * vtn <= lim, T(M.ct), lim / vtn);
-  *mimp = T(M.dt) * T(M.imp_c) * s;
+  *mimp = m_mul2_c(s, M.dt, M.imp_c, M.dt_imp_c);
   return v3(-scale * v.x, -scale * v.y, fn);
 }
 
@@ -559,7 +565,7 @@ template <class T> SPI_INL T joint_target(const DevModel& M, int k, int leg, T a
 // Motor torque of joint k towards its position target.
 template <class T> SPI_INL T motor_torque_at(const DevModel& M, const LegParams<T>& P, int k, int leg,
                                              T target, T q, T qd) {
-  T tau = P.kps * T(M.kp[k][leg]) * (target - q) - T(M.kd_scale) * T(M.kd[k][leg]) * qd;
+  T tau = P.kps * T(M.kp[k][leg]) * (target - q) - m_mul2_c(qd, M.kd_scale, M.kd[k][leg], M.kdd[k][leg]);
   T lim = P.ts * T(M.tlim[k][leg]);
   if (M.torque_speed) lim = lim * m_fmax(T(0), T(1) - m_div_c(m_fabs(qd), M.vlim[k][leg], M.vlim_inv[k][leg]));
   tau = m_clamp(tau, -lim, lim) * T(M.gain[k]);

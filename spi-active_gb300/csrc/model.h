@@ -27,6 +27,7 @@ inline int build_dev_model(const spi_robot& r, DevModel* M, const char** why) {
       M->tlim[k][leg] = r.torque_limit[b];
       M->vlim[k][leg] = r.velocity_limit[b];
       M->vlim_inv[k][leg] = r.torque_speed ? (float)(1.0 / (double)r.velocity_limit[b]) : 0.0f;
+      M->kdd[k][leg] = r.kd_scale * r.kd[b];
       if (!(r.body_mass[b] > 0.0f)) { *why = "leg body mass must be > 0"; return SPI_EINVAL; }
       // the kernel's transforms assume thigh joints offset along y and calf joints along z
       if (k == 1 && (r.body_origin[b][0] != 0.0f || r.body_origin[b][2] != 0.0f)) {
@@ -62,6 +63,7 @@ inline int build_dev_model(const spi_robot& r, DevModel* M, const char** why) {
   if (!(r.contact_ramp > 0.0f)) { *why = "contact_ramp must be > 0"; return SPI_EINVAL; }
   M->ramp_inv = 1.0f / r.contact_ramp;
   M->imp_c = r.contact_c > r.contact_ct ? r.contact_c : r.contact_ct;
+  M->dt_imp_c = r.sim_dt * M->imp_c;
   M->kd_scale = r.kd_scale; M->act_scale = r.action_scale; M->act_clip = r.action_clip;
   M->hip_scale = r.hip_action_scale; M->fric_vel = r.friction_vel;
   M->dt = r.sim_dt; M->g = r.gravity;
