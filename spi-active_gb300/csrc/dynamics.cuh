@@ -474,7 +474,29 @@ template <class T> struct BaseState {
 };
 template <class T> struct LegState { T q[3], qd[3]; };
 template <class T> struct BaseParams { T m; V3<T> h; S3<T> Io; };   // base rigid inertia (+ fixed links)
-template <class T> struct LegParams { T kps, fc, arm, ts; };        // leg group's motor terms
+template <class T> struct LegParams {                                // leg group's motor terms
+  T kps, fc, arm, ts;
+  // joint k's stiffness kps kp and torque limit ts tlim
+  SPI_INL T kp_of(const DevModel& M, int k, int leg) const { return kps * T(M.kp[k][leg]); }
+  SPI_INL T lim_of(const DevModel& M, int k, int leg) const { return ts * T(M.tlim[k][leg]); }
+};
+// One leg's motor terms with the per-joint products formed once (theta is fixed over a
+// rollout): the same members as LegParams, for phase A's per-leg loop.
+template <class T> struct LegGains {
+  T kpk[3], lim[3], fc, arm;
+  SPI_INL T kp_of(const DevModel&, int k, int) const { return kpk[k]; }
+  SPI_INL T lim_of(const DevModel&, int k, int) const { return lim[k]; }
+};
+template <class T> SPI_INL LegGains<T> leg_gains(const DevModel& M, const LegParams<T>& P, int leg) {
+  LegGains<T> g;
+  for (int k = 0; k < 3; ++k) {
+    g.kpk[k] = P.kp_of(M, k, leg);
+    g.lim[k] = P.lim_of(M, k, leg);
+  }
+  g.fc = P.fc;
+  g.arm = P.arm;
+  return g;
+}
 template <class T> struct LegOut { Art<T> I; SV<T> p; };            // leg contribution at the base
 // Phase A -> phase C. The leg's joint-space inertia factors as M = L D L^T (L unit lower
 // triangular: l10, l20, l21), the coupling to the base as K = F L^-T (F = the joints' spatial
@@ -563,10 +585,10 @@ template <class T> SPI_INL T joint_target(const DevModel& M, int k, int leg, T a
   return a + T(M.q0[k][leg]);
 }
 // Motor torque of joint k towards its position target.
-template <class T> SPI_INL T motor_torque_at(const DevModel& M, const LegParams<T>& P, int k, int leg,
-                                             T target, T q, T qd) {
-  T tau = P.kps * T(M.kp[k][leg]) * (target - q) - m_mul2_c(qd, M.kd_scale, M.kd[k][leg], M.kdd[k][leg]);
-  T lim = P.ts * T(M.tlim[k][leg]);
+template <class T, class PT> SPI_INL T motor_torque_at(const DevModel& M, const PT& P, int k, int leg,
+                                                       T target, T q, T qd) {
+  T tau = P.kp_of(M, k, leg) * (target - q) - m_mul2_c(qd, M.kd_scale, M.kd[k][leg], M.kdd[k][leg]);
+  T lim = P.lim_of(M, k, leg);
   if (M.torque_speed) lim = lim * m_fmax(T(0), T(1) - m_div_c(m_fabs(qd), M.vlim[k][leg], M.vlim_inv[k][leg]));
   tau = m_clamp(tau, -lim, lim) * T(M.gain[k]);
   if (M.tanh_a[k] > 0.0f) tau = T(M.tanh_a[k]) * m_tanh(tau / T(M.tanh_a[k]));
@@ -634,9 +656,10 @@ template <class T> SPI_INL void art_sub_outer(Art<T>& I, const SV<T>& a, const S
 // ACC = false: out receives the leg's contribution; ACC = true: the contribution is added to out
 // (the running sum over legs, which may start from the base body's own terms).
 // TGT = false: act holds the leg's three actions; TGT = true: their joint targets (joint_target).
-template <bool ACC, bool TGT, class T, class WK>
+// PT: LegParams, or LegGains.
+template <bool ACC, bool TGT, class T, class WK, class PT>
 SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
-                          const LegParams<T>& P, const T act[3], WK& W, LegOut<T>& out) {
+                          const PT& P, const T act[3], WK& W, LegOut<T>& out) {
   T tau[3], C[3], S[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -759,9 +782,9 @@ SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, con
 }
 // Phase A adding the leg's contribution to acc, from the leg's joint targets tgt (joint_target
 // of its three actions, formed once per control step).
-template <class T, class WK>
+template <class T, class WK, class PT>
 SPI_INL void phase_a_into(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
-                          const LegParams<T>& P, const T tgt[3], WK& W, LegOut<T>& acc) {
+                          const PT& P, const T tgt[3], WK& W, LegOut<T>& acc) {
   phase_a_core<true, true>(M, leg, B, L, P, tgt, W, acc);
 }
 

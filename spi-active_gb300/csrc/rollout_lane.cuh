@@ -96,18 +96,32 @@ struct LaneSlots {
   }
 };
 
-// One physics substep of one rollout on one lane. s: this thread's slots; bp / lp: the warp's
-// base and (front, rear) leg parameters.
+// A leg's LegGains as two 16-byte fields (kpk 3, lim 3, fc, arm).
+__device__ __forceinline__ LegGains<float> load_gains(const float4* g) {
+  const float4 a = g[0], b = g[1];
+  LegGains<float> r;
+  r.kpk[0] = a.x; r.kpk[1] = a.y; r.kpk[2] = a.z;
+  r.lim[0] = a.w; r.lim[1] = b.x; r.lim[2] = b.y;
+  r.fc = b.z; r.arm = b.w;
+  return r;
+}
+__device__ __forceinline__ void store_gains(const LegGains<float>& r, float4* g) {
+  g[0] = make_float4(r.kpk[0], r.kpk[1], r.kpk[2], r.lim[0]);
+  g[1] = make_float4(r.lim[1], r.lim[2], r.fc, r.arm);
+}
+
+// One physics substep of one rollout on one lane. s: this thread's slots; bp: the warp's base
+// parameters; gains: the warp's four legs' LegGains (two fields each).
 template <bool PEEL>
 __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>& B, const LaneSlots& s,
-                                             const BaseParams<float>* bp, const LegParams<float>* lp) {
+                                             const BaseParams<float>* bp, const float4* gains) {
   constexpr int NP = PEEL ? 3 : 4;
   // articulated inertia and bias force at the base: the base body's own, plus each leg's
   LegOut<float> sum = base_terms(*bp, B);
   const float4* tgt = s.sm + lane_act<PEEL>() * 128;
 #pragma unroll 1
   for (int leg = 0; leg < NP; ++leg) {
-    const LegParams<float> P = lp[leg >> 1];
+    const LegGains<float> P = load_gains(gains + 2 * leg);
     const float4 a = tgt[leg * 128];
     const float a3[3] = {a.x, a.y, a.z};
     ParkedWork pw{s.park(leg), 128};
@@ -116,7 +130,7 @@ __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>
   LegWork<float> w3;
   if (PEEL) {
     const float a3[3] = {tgt[0].w, tgt[128].w, tgt[256].w};
-    phase_a_into(M, 3, B, s.leg_state<PEEL>(3), lp[1], a3, w3, sum);
+    phase_a_into(M, 3, B, s.leg_state<PEEL>(3), load_gains(gains + 6), a3, w3, sum);
   }
   const SV<float> a0 = base_solve(M, sum.I, sum.p, B);
   if (PEEL) {
@@ -136,13 +150,13 @@ __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>
 
 // One warp: theta th13 against windows [32 wb, 32 wb + 32) of win, writing the partials of the
 // four eight-window groups g = 4 wb .. 4 wb + 3 (those below G) to partial_n[g][SPI_N_COMP].
-// lane_smem: the CTA's lane_smem_bytes<PEEL>() of dynamic shared memory; bp_warp / lp_warp: the CTA's
-// per-warp parameter slots. Callable repeatedly by one warp (persistent kernels).
+// lane_smem: the CTA's lane_smem_bytes<PEEL>() of dynamic shared memory; bp_warp / gains_warp: the
+// CTA's per-warp parameter slots. Callable repeatedly by one warp (persistent kernels).
 template <bool PEEL>
 __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinView& win, const float* th13, int wb,
                                                   float* partial_n, int G, unsigned long long* n_bad,
                                                   float4* lane_smem, BaseParams<float>* bp_warp,
-                                                  LegParams<float> (*lp_warp)[2]) {
+                                                  float4 (*gains_warp)[8]) {
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int W = win.W, H = win.H;
   int w = wb * 32 + lane;
@@ -154,11 +168,8 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
     float th[SPI_THETA_DIM];
 #pragma unroll
     for (int i = 0; i < SPI_THETA_DIM; ++i) th[i] = __ldg(th13 + i);
-    if (lane == 0) {
-      bp_warp[wib] = base_params<float>(M, th);
-      lp_warp[wib][0] = leg_params<float>(th, 0);
-      lp_warp[wib][1] = leg_params<float>(th, 2);
-    }
+    if (lane == 0) bp_warp[wib] = base_params<float>(M, th);
+    if (lane < 4) store_gains(leg_gains(M, leg_params<float>(th, lane), lane), gains_warp[wib] + 2 * lane);
     __syncwarp();
   }
 
@@ -184,7 +195,7 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
   for (int h = 0; h < H; ++h) {
     const float4* ap = reinterpret_cast<const float4*>(win.act + ((size_t)h * W + w) * 12);
     sl.put_targets<PEEL>(M, __ldg(ap), __ldg(ap + 1), __ldg(ap + 2));
-    for (int s = 0; s < dec; ++s) substep_lane<PEEL>(M, B, sl, &bp_warp[wib], lp_warp[wib]);
+    for (int s = 0; s < dec; ++s) substep_lane<PEEL>(M, B, sl, &bp_warp[wib], gains_warp[wib]);
   }
   LegState<float> L[4];
 #pragma unroll
@@ -232,13 +243,13 @@ __global__ void __launch_bounds__(128, MINB) rollout_lane_kernel(const __grid_co
                                                                  unsigned long long* __restrict__ n_bad) {
   extern __shared__ float4 lane_smem[];              // lane_smem_bytes<(MINB >= 4)>()
   __shared__ BaseParams<float> bp_warp[4];
-  __shared__ LegParams<float> lp_warp[4][2];
+  __shared__ float4 gains_warp[4][8];
   const int WB = (win.W + 31) >> 5;
   const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (warp >= (long long)N * WB) return;   // uniform per warp
   const int n = (int)(warp / WB), wb = (int)(warp % WB);
   rollout_lane_warp<(MINB >= 4)>(M, win, theta + (size_t)n * SPI_THETA_DIM, wb, partial + (size_t)n * G * SPI_N_COMP,
-                                 G, n_bad, lane_smem, bp_warp, lp_warp);
+                                 G, n_bad, lane_smem, bp_warp, gains_warp);
 }
 
 }  // namespace spi

@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(128, MINB) server_rollout_lane_kernel(const __
                                                                   int max_slots, int round) {
   extern __shared__ float4 lane_smem[];              // kLaneParkBytes
   __shared__ BaseParams<float> bp_warp[4];
-  __shared__ LegParams<float> lp_warp[4][2];
+  __shared__ float4 gains_warp[4][8];
   const int lane = threadIdx.x & 31;
   const TickInfo* info = info_all + round;
   const int* order = order_all + (size_t)round * max_slots;
@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(128, MINB) server_rollout_lane_kernel(const __
       const int WB = (S.win.W + 31) >> 5;
       const int n = (int)(local / WB), wb = (int)(local % WB);
       rollout_lane_warp<false>(M, S.win, S.theta + (size_t)n * SPI_THETA_DIM, wb,
-                               S.partial + (size_t)n * S.G * SPI_N_COMP, S.G, n_bad, lane_smem, bp_warp, lp_warp);
+                               S.partial + (size_t)n * S.G * SPI_N_COMP, S.G, n_bad, lane_smem, bp_warp, gains_warp);
     }
   }
 }
