@@ -439,16 +439,25 @@ template <int AX, int RM, class T> SPI_INL RI<T> ri_to_parent(const RI<T>& c, T 
 // ---------------------------------------------------------------------------
 // model constants as the kernel sees them (built on the host from spi_robot)
 // ---------------------------------------------------------------------------
+struct alignas(16) F4 { float x, y, z, w; };
+constexpr int kLegSlots = 14;
+
 struct DevModel {
-  // per leg body k (0 hip, 1 thigh, 2 calf), component, leg: [k][c][leg] keeps the four
-  // legs' copies of one constant in four consecutive shared-memory banks
+  // The per-leg constants phase A reads, leg-major, four to a 16-byte slot, so that one leg's
+  // are contiguous (one 128-bit load per slot) and the four legs' copies of a slot sit 56
+  // words apart (distinct shared-memory banks when lanes of one quad read the four legs):
+  //   0..2   joint k: origin x, y, z, kd_scale kd (float product)
+  //   3..11  body b at 3 + 3 b: (m, h x, h y, h z), (Ixx, Iyy, Izz, Ixy), (Ixz, Iyz, 1 / vlim_b, 0)
+  //          (1 / vlim is 0 without the torque-speed limit)
+  //   12, 13 the leg's two base-box corners: (c0 x, c0 y, c0 z, c1 x), (c1 y, c1 z, 0, 0)
+  F4 legc[4][kLegSlots];
+  // per leg body k (0 hip, 1 thigh, 2 calf), component, leg: [k][c][leg] (the same constants
+  // as the source arrays of legc, for the host-side formulations)
   float org[3][3][4];
   float m[3][4];
   float h[3][3][4];
   float I[3][6][4];   // xx yy zz xy xz yz about the body origin
   float kp[3][4], kd[3][4], q0[3][4], tlim[3][4], vlim[3][4];
-  float vlim_inv[3][4];   // 1 / vlim (0 without the torque-speed limit)
-  float kdd[3][4];        // kd_scale kd (float product)
   float corner[8][3];
   float foot[3];
   float gain[3], tanh_a[3];
@@ -587,9 +596,10 @@ template <class T> SPI_INL T joint_target(const DevModel& M, int k, int leg, T a
 // Motor torque of joint k towards its position target.
 template <class T, class PT> SPI_INL T motor_torque_at(const DevModel& M, const PT& P, int k, int leg,
                                                        T target, T q, T qd) {
-  T tau = P.kp_of(M, k, leg) * (target - q) - m_mul2_c(qd, M.kd_scale, M.kd[k][leg], M.kdd[k][leg]);
+  const F4* lc = M.legc[leg];
+  T tau = P.kp_of(M, k, leg) * (target - q) - m_mul2_c(qd, M.kd_scale, M.kd[k][leg], lc[k].w);
   T lim = P.lim_of(M, k, leg);
-  if (M.torque_speed) lim = lim * m_fmax(T(0), T(1) - m_div_c(m_fabs(qd), M.vlim[k][leg], M.vlim_inv[k][leg]));
+  if (M.torque_speed) lim = lim * m_fmax(T(0), T(1) - m_div_c(m_fabs(qd), M.vlim[k][leg], lc[5 + 3 * k].z));
   tau = m_clamp(tau, -lim, lim) * T(M.gain[k]);
   if (M.tanh_a[k] > 0.0f) tau = T(M.tanh_a[k]) * m_tanh(tau / T(M.tanh_a[k]));
   return tau - P.fc * m_tanh_div(qd, M.fric_vel, M.fric_k2);
@@ -609,6 +619,20 @@ template <class T> SPI_INL RI<T> leg_ri(const DevModel& M, int k, int leg) {
   r.I.xx = T(M.I[k][0][leg]); r.I.yy = T(M.I[k][1][leg]); r.I.zz = T(M.I[k][2][leg]);
   r.I.xy = T(M.I[k][3][leg]); r.I.xz = T(M.I[k][4][leg]); r.I.yz = T(M.I[k][5][leg]);
   return r;
+}
+
+// The same constants from a leg's packed slots (DevModel::legc).
+template <class T> SPI_INL V3<T> lc_org(const F4* c, int k) { return v3(T(c[k].x), T(c[k].y), T(c[k].z)); }
+template <class T> SPI_INL RI<T> lc_ri(const F4* c, int b) {
+  const F4 a = c[3 + 3 * b], d = c[4 + 3 * b], e = c[5 + 3 * b];
+  RI<T> r;
+  r.m = T(a.x);
+  r.h = v3(T(a.y), T(a.z), T(a.w));
+  r.I.xx = T(d.x); r.I.yy = T(d.y); r.I.zz = T(d.z); r.I.xy = T(d.w); r.I.xz = T(e.x); r.I.yz = T(e.y);
+  return r;
+}
+template <class T> SPI_INL V3<T> lc_corner(const F4* c, int j) {
+  return j == 0 ? v3(T(c[12].x), T(c[12].y), T(c[12].z)) : v3(T(c[12].w), T(c[13].x), T(c[13].y));
 }
 
 // c = v x (S qd) for a revolute joint about axis AX.
@@ -666,7 +690,8 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
     tau[k] = motor_torque_at(M, P, k, leg, TGT ? act[k] : joint_target(M, k, leg, act[k]), L.q[k], L.qd[k]);
     m_sincos(L.q[k], &S[k], &C[k]);
   }
-  V3<T> r0 = leg_org<T>(M, 0, leg), r1 = leg_org<T>(M, 1, leg), r2 = leg_org<T>(M, 2, leg);
+  const F4* lc = M.legc[leg];
+  V3<T> r0 = lc_org<T>(lc, 0), r1 = lc_org<T>(lc, 1), r2 = lc_org<T>(lc, 2);
   // body velocities (body coordinates) and velocity-product accelerations
   SV<T> v0 = motion_to_child<0>(B.nu, C[0], S[0], r0); v0.w.x = v0.w.x + L.qd[0];
   SV<T> v1 = motion_to_child<1, 2>(v0, C[1], S[1], r1);   v1.w.y = v1.w.y + L.qd[1];
@@ -693,11 +718,11 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   Fc = rotT<1>(C[1], S[1], Fc);
   Fc = rotT<1>(C[2], S[2], Fc);
   // composite inertias: calf (+ the contact's implicit point mass at the foot) -> thigh -> hip
-  const RI<T> Ical = leg_ri<T>(M, 2, leg);
+  const RI<T> Ical = lc_ri<T>(lc, 2);
   RI<T> Rc2 = Ical;
   ri_add_point(Rc2, mimp, fc);
-  const RI<T> Rc1 = ri_to_parent_acc<1, 4>(Rc2, C[2], S[2], r2, leg_ri<T>(M, 1, leg));
-  const RI<T> Rc0 = ri_to_parent_acc<1, 2>(Rc1, C[1], S[1], r1, leg_ri<T>(M, 0, leg));
+  const RI<T> Rc1 = ri_to_parent_acc<1, 4>(Rc2, C[2], S[2], r2, lc_ri<T>(lc, 1));
+  const RI<T> Rc0 = ri_to_parent_acc<1, 2>(Rc1, C[1], S[1], r1, lc_ri<T>(lc, 0));
   // bias pass (a0 = 0, qdd = 0): accelerations are the accumulated velocity products; the
   // implicit point mass takes part in the inertial force, not in the velocity term
   const SV<T> ab1 = motion_to_child_acc<1, 2>(cb0, C[1], S[1], r1, cb1);
@@ -707,12 +732,12 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   f2.v = f2.v - Fc;
   SV<T> f1;
   {
-    const RI<T> Ith = leg_ri<T>(M, 1, leg);
+    const RI<T> Ith = lc_ri<T>(lc, 1);
     f1 = ri_mul_acc(Ith, ab1, crf_acc(v1, ri_mul(Ith, v1), force_to_parent<1, 4>(f2, C[2], S[2], r2)));
   }
   SV<T> f0;
   {
-    const RI<T> Ihp = leg_ri<T>(M, 0, leg);
+    const RI<T> Ihp = lc_ri<T>(lc, 0);
     f0 = ri_mul_acc(Ihp, cb0, crf_acc(v0, ri_mul(Ihp, v0), force_to_parent<1, 2>(f1, C[1], S[1], r1)));
   }
   const SV<T> pc = ACC ? force_to_parent_acc<0, 7>(f0, C[0], S[0], r0, out.p) : force_to_parent<0, 7>(f0, C[0], S[0], r0);
@@ -758,8 +783,7 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   if (M.base_contact && warp_any(B.p.z < T(M.corner_reach))) {
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
-      const float* cc = M.corner[2 * leg + j];
-      V3<T> rc = v3(T(cc[0]), T(cc[1]), T(cc[2]));
+      const V3<T> rc = lc_corner<T>(lc, j);
       V3<T> vc = cross_acc(B.nu.w, rc, B.nu.v);
       T mc;
       V3<T> Fw = contact_force(M, T(0), B.p.z + B.R.m[2][0] * rc.x + B.R.m[2][1] * rc.y + B.R.m[2][2] * rc.z,

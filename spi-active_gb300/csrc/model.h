@@ -26,8 +26,12 @@ inline int build_dev_model(const spi_robot& r, DevModel* M, const char** why) {
       M->q0[k][leg] = r.default_q[b];
       M->tlim[k][leg] = r.torque_limit[b];
       M->vlim[k][leg] = r.velocity_limit[b];
-      M->vlim_inv[k][leg] = r.torque_speed ? (float)(1.0 / (double)r.velocity_limit[b]) : 0.0f;
-      M->kdd[k][leg] = r.kd_scale * r.kd[b];
+      F4* lc = M->legc[leg];
+      lc[k] = F4{r.body_origin[b][0], r.body_origin[b][1], r.body_origin[b][2], r.kd_scale * r.kd[b]};
+      lc[3 + 3 * k] = F4{r.body_mass[b], r.body_h[b][0], r.body_h[b][1], r.body_h[b][2]};
+      lc[4 + 3 * k] = F4{r.body_I[b][0], r.body_I[b][1], r.body_I[b][2], r.body_I[b][3]};
+      lc[5 + 3 * k] = F4{r.body_I[b][4], r.body_I[b][5],
+                         r.torque_speed ? (float)(1.0 / (double)r.velocity_limit[b]) : 0.0f, 0.0f};
       if (!(r.body_mass[b] > 0.0f)) { *why = "leg body mass must be > 0"; return SPI_EINVAL; }
       // the kernel's transforms assume thigh joints offset along y and calf joints along z
       if (k == 1 && (r.body_origin[b][0] != 0.0f || r.body_origin[b][2] != 0.0f)) {
@@ -42,6 +46,12 @@ inline int build_dev_model(const spi_robot& r, DevModel* M, const char** why) {
     }
   }
   memcpy(M->corner, r.corners, sizeof(M->corner));
+  for (int leg = 0; leg < 4; ++leg) {
+    const float* c0 = r.corners[2 * leg];
+    const float* c1 = r.corners[2 * leg + 1];
+    M->legc[leg][12] = F4{c0[0], c0[1], c0[2], c1[0]};
+    M->legc[leg][13] = F4{c1[1], c1[2], 0.0f, 0.0f};
+  }
   M->corner_reach = 0.0f;
   for (int i = 0; i < 8; ++i) {
     const float d = sqrtf(r.corners[i][0] * r.corners[i][0] + r.corners[i][1] * r.corners[i][1] +
