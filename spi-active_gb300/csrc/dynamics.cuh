@@ -677,13 +677,20 @@ template <class T> SPI_INL void art_sub_outer(Art<T>& I, const SV<T>& a, const S
 // base, I_c - F M^-1 F^T and p_c + F M^-1 (tau - C) -- the quantities Featherstone's ABA
 // backward pass produces, from fewer operations for a three-joint chain.
 // ---------------------------------------------------------------------------
+// Whether phase A evaluates the base-box corners: a corner can only reach the ground when the
+// base origin is lower than the box's half-diagonal, so a warp whose rollouts are all higher
+// skips them. One vote per warp and base state, shared by the four legs.
+template <class T> SPI_INL bool corners_may_touch(const DevModel& M, const BaseState<T>& B) {
+  return M.base_contact && warp_any(B.p.z < T(M.corner_reach));
+}
+
 // ACC = false: out receives the leg's contribution; ACC = true: the contribution is added to out
 // (the running sum over legs, which may start from the base body's own terms).
 // TGT = false: act holds the leg's three actions; TGT = true: their joint targets (joint_target).
 // PT: LegParams, or LegGains.
 template <bool ACC, bool TGT, class T, class WK, class PT>
 SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
-                          const PT& P, const T act[3], WK& W, LegOut<T>& out) {
+                          const PT& P, const T act[3], WK& W, LegOut<T>& out, bool corners) {
   T tau[3], C[3], S[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -777,10 +784,9 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
                pc.w.z + y2 * K2.w.z + y1 * K1.w.z + y0 * K0.w.z);
   out.p.v = v3(pc.v.x + y2 * K2.v.x + y1 * K1.v.x + y0 * K0.v.x, pc.v.y + y2 * K2.v.y + y1 * K1.v.y + y0 * K0.v.y,
                pc.v.z + y2 * K2.v.z + y1 * K1.v.z + y0 * K0.v.z);
-  // two of the eight base-box corners; a corner can only reach the ground when the base origin
-  // is lower than the box's half-diagonal, so a warp whose rollouts are all higher skips them
-  // (a corner off the ground adds exactly zero force and zero implicit mass)
-  if (M.base_contact && warp_any(B.p.z < T(M.corner_reach))) {
+  // two of the eight base-box corners, when corners_may_touch (a corner off the ground adds
+  // exactly zero force and zero implicit mass)
+  if (corners) {
 #pragma unroll
     for (int j = 0; j < 2; ++j) {
       const V3<T> rc = lc_corner<T>(lc, j);
@@ -801,15 +807,15 @@ template <class T, class WK>
 SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
                           const LegParams<T>& P, const T act[3], WK& W) {
   LegOut<T> out;
-  phase_a_core<false, false>(M, leg, B, L, P, act, W, out);
+  phase_a_core<false, false>(M, leg, B, L, P, act, W, out, corners_may_touch(M, B));
   return out;
 }
 // Phase A adding the leg's contribution to acc, from the leg's joint targets tgt (joint_target
-// of its three actions, formed once per control step).
+// of its three actions, formed once per control step); corners: corners_may_touch(M, B).
 template <class T, class WK, class PT>
 SPI_INL void phase_a_into(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
-                          const PT& P, const T tgt[3], WK& W, LegOut<T>& acc) {
-  phase_a_core<true, true>(M, leg, B, L, P, tgt, W, acc);
+                          const PT& P, const T tgt[3], WK& W, LegOut<T>& acc, bool corners) {
+  phase_a_core<true, true>(M, leg, B, L, P, tgt, W, acc, corners);
 }
 
 // ---------------------------------------------------------------------------

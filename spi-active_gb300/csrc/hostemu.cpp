@@ -67,7 +67,8 @@ static void substep(const DevModel& M, BaseState<T>& B, LegState<T> L[4], const 
   } else {
     // as the lane-per-rollout kernel: the legs summed onto the base body's own terms in order
     LegOut<T> sum = base_terms(bp, B);
-    for (int leg = 0; leg < 4; ++leg) phase_a_into(M, leg, B, L[leg], lp[leg], act + 3 * leg, W[leg], sum);
+    const bool corners = corners_may_touch(M, B);
+    for (int leg = 0; leg < 4; ++leg) phase_a_into(M, leg, B, L[leg], lp[leg], act + 3 * leg, W[leg], sum, corners);
     a0 = base_solve(M, sum.I, sum.p, B);
   }
   for (int leg = 0; leg < 4; ++leg) {
@@ -200,7 +201,8 @@ int spi_hostemu_count_phases(const spi_robot* robot, const double* state, const 
   LegWork<Cf> W[4];
   Cf::n = 0;
   LegOut<Cf> sum = base_terms(bp, B);
-  for (int leg = 0; leg < 4; ++leg) phase_a_into(M, leg, B, L[leg], lp[leg], act + 3 * leg, W[leg], sum);
+  const bool corners = corners_may_touch(M, B);
+  for (int leg = 0; leg < 4; ++leg) phase_a_into(M, leg, B, L[leg], lp[leg], act + 3 * leg, W[leg], sum, corners);
   out3[0] = Cf::n;
   Cf::n = 0;
   SV<Cf> a0 = base_solve(M, sum.I, sum.p, B);

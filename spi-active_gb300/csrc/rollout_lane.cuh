@@ -119,18 +119,19 @@ __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>
   // articulated inertia and bias force at the base: the base body's own, plus each leg's
   LegOut<float> sum = base_terms(*bp, B);
   const float4* tgt = s.sm + lane_act<PEEL>() * 128;
+  const bool corners = corners_may_touch(M, B);
 #pragma unroll 1
   for (int leg = 0; leg < NP; ++leg) {
     const LegGains<float> P = load_gains(gains + 2 * leg);
     const float4 a = tgt[leg * 128];
     const float a3[3] = {a.x, a.y, a.z};
     ParkedWork pw{s.park(leg), 128};
-    phase_a_into(M, leg, B, s.leg_state<PEEL>(leg), P, a3, pw, sum);
+    phase_a_into(M, leg, B, s.leg_state<PEEL>(leg), P, a3, pw, sum, corners);
   }
   LegWork<float> w3;
   if (PEEL) {
     const float a3[3] = {tgt[0].w, tgt[128].w, tgt[256].w};
-    phase_a_into(M, 3, B, s.leg_state<PEEL>(3), load_gains(gains + 6), a3, w3, sum);
+    phase_a_into(M, 3, B, s.leg_state<PEEL>(3), load_gains(gains + 6), a3, w3, sum, corners);
   }
   const SV<float> a0 = base_solve(M, sum.I, sum.p, B);
   if (PEEL) {
