@@ -594,14 +594,30 @@ template <class T> SPI_INL T joint_target(const DevModel& M, int k, int leg, T a
   return a + T(M.q0[k][leg]);
 }
 // Motor torque of joint k towards its position target.
-template <class T, class PT> SPI_INL T motor_torque_at(const DevModel& M, const PT& P, int k, int leg,
-                                                       T target, T q, T qd) {
+// Motor-model shape known at compile time. kMotorRuntime: the model's flags are read at run time;
+// kMotorSpeedLimit: torque-speed limit on, unit gains, no tanh saturation (motor_shape_of
+// picks it for such a model; the results are the same, the flags' tests and the unit-gain
+// multiplies are left out).
+constexpr int kMotorRuntime = 0;
+constexpr int kMotorSpeedLimit = 1;
+inline int motor_shape_of(const DevModel& M) {
+  for (int k = 0; k < 3; ++k)
+    if (M.gain[k] != 1.0f || M.tanh_a[k] > 0.0f) return kMotorRuntime;
+  return M.torque_speed ? kMotorSpeedLimit : kMotorRuntime;
+}
+
+template <int MS = kMotorRuntime, class T, class PT>
+SPI_INL T motor_torque_at(const DevModel& M, const PT& P, int k, int leg, T target, T q, T qd) {
   const F4* lc = M.legc[leg];
   T tau = P.kp_of(M, k, leg) * (target - q) - m_mul2_c(qd, M.kd_scale, M.kd[k][leg], lc[k].w);
   T lim = P.lim_of(M, k, leg);
-  if (M.torque_speed) lim = lim * m_fmax(T(0), T(1) - m_div_c(m_fabs(qd), M.vlim[k][leg], lc[5 + 3 * k].z));
-  tau = m_clamp(tau, -lim, lim) * T(M.gain[k]);
-  if (M.tanh_a[k] > 0.0f) tau = T(M.tanh_a[k]) * m_tanh(tau / T(M.tanh_a[k]));
+  if (MS == kMotorSpeedLimit || M.torque_speed)
+    lim = lim * m_fmax(T(0), T(1) - m_div_c(m_fabs(qd), M.vlim[k][leg], lc[5 + 3 * k].z));
+  tau = m_clamp(tau, -lim, lim);
+  if (MS == kMotorRuntime) {
+    tau = tau * T(M.gain[k]);
+    if (M.tanh_a[k] > 0.0f) tau = T(M.tanh_a[k]) * m_tanh(tau / T(M.tanh_a[k]));
+  }
   return tau - P.fc * m_tanh_div(qd, M.fric_vel, M.fric_k2);
 }
 template <class T> SPI_INL T motor_torque(const DevModel& M, const LegParams<T>& P, int k, int leg,
@@ -688,13 +704,13 @@ template <class T> SPI_INL bool corners_may_touch(const DevModel& M, const BaseS
 // (the running sum over legs, which may start from the base body's own terms).
 // TGT = false: act holds the leg's three actions; TGT = true: their joint targets (joint_target).
 // PT: LegParams, or LegGains.
-template <bool ACC, bool TGT, class T, class WK, class PT>
+template <bool ACC, bool TGT, int MS, class T, class WK, class PT>
 SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
                           const PT& P, const T act[3], WK& W, LegOut<T>& out, bool corners) {
   T tau[3], C[3], S[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    tau[k] = motor_torque_at(M, P, k, leg, TGT ? act[k] : joint_target(M, k, leg, act[k]), L.q[k], L.qd[k]);
+    tau[k] = motor_torque_at<MS>(M, P, k, leg, TGT ? act[k] : joint_target(M, k, leg, act[k]), L.q[k], L.qd[k]);
     m_sincos(L.q[k], &S[k], &C[k]);
   }
   const F4* lc = M.legc[leg];
@@ -807,15 +823,16 @@ template <class T, class WK>
 SPI_INL LegOut<T> phase_a(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
                           const LegParams<T>& P, const T act[3], WK& W) {
   LegOut<T> out;
-  phase_a_core<false, false>(M, leg, B, L, P, act, W, out, corners_may_touch(M, B));
+  phase_a_core<false, false, kMotorRuntime>(M, leg, B, L, P, act, W, out, corners_may_touch(M, B));
   return out;
 }
 // Phase A adding the leg's contribution to acc, from the leg's joint targets tgt (joint_target
 // of its three actions, formed once per control step); corners: corners_may_touch(M, B).
-template <class T, class WK, class PT>
+// MS: the motor shape (motor_shape_of the model, or kMotorRuntime).
+template <int MS = kMotorRuntime, class T, class WK, class PT>
 SPI_INL void phase_a_into(const DevModel& M, int leg, const BaseState<T>& B, const LegState<T>& L,
                           const PT& P, const T tgt[3], WK& W, LegOut<T>& acc, bool corners) {
-  phase_a_core<true, true>(M, leg, B, L, P, tgt, W, acc, corners);
+  phase_a_core<true, true, MS>(M, leg, B, L, P, tgt, W, acc, corners);
 }
 
 // ---------------------------------------------------------------------------

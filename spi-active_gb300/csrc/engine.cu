@@ -74,6 +74,9 @@ int spi::run_impl(spi_engine* e, float* trace) {
     if (e->min_blocks <= 2)
       rollout_lane_kernel<2><<<lgrid, 128, kLaneParkBytes, e->stream>>>(e->host_model, win, e->theta.f(), e->N, G,
                                                                         e->partial.f(), bad);
+    else if (e->min_blocks == 3 && motor_shape_of(e->host_model) == kMotorSpeedLimit)
+      rollout_lane_kernel<3, kMotorSpeedLimit><<<lgrid, 128, kLaneParkBytes, e->stream>>>(
+          e->host_model, win, e->theta.f(), e->N, G, e->partial.f(), bad);
     else if (e->min_blocks == 3)
       rollout_lane_kernel<3><<<lgrid, 128, kLaneParkBytes, e->stream>>>(e->host_model, win, e->theta.f(), e->N, G,
                                                                         e->partial.f(), bad);
@@ -224,6 +227,9 @@ int spi_set_kernel_layout(spi_engine* e, int layout) {
     if (ce == cudaSuccess)
       ce = cudaFuncSetAttribute(rollout_lane_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 kLaneParkBytes);
+    if (ce == cudaSuccess)
+      ce = cudaFuncSetAttribute(rollout_lane_kernel<3, kMotorSpeedLimit>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, kLaneParkBytes);
     if (ce == cudaSuccess)
       ce = cudaFuncSetAttribute(rollout_lane_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 kLanePeelBytes);

@@ -112,7 +112,7 @@ __device__ __forceinline__ void store_gains(const LegGains<float>& r, float4* g)
 
 // One physics substep of one rollout on one lane. s: this thread's slots; bp: the warp's base
 // parameters; gains: the warp's four legs' LegGains (two fields each).
-template <bool PEEL>
+template <bool PEEL, int MS>
 __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>& B, const LaneSlots& s,
                                              const BaseParams<float>* bp, const float4* gains) {
   constexpr int NP = PEEL ? 3 : 4;
@@ -126,12 +126,12 @@ __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>
     const float4 a = tgt[leg * 128];
     const float a3[3] = {a.x, a.y, a.z};
     ParkedWork pw{s.park(leg), 128};
-    phase_a_into(M, leg, B, s.leg_state<PEEL>(leg), P, a3, pw, sum, corners);
+    phase_a_into<MS>(M, leg, B, s.leg_state<PEEL>(leg), P, a3, pw, sum, corners);
   }
   LegWork<float> w3;
   if (PEEL) {
     const float a3[3] = {tgt[0].w, tgt[128].w, tgt[256].w};
-    phase_a_into(M, 3, B, s.leg_state<PEEL>(3), load_gains(gains + 6), a3, w3, sum, corners);
+    phase_a_into<MS>(M, 3, B, s.leg_state<PEEL>(3), load_gains(gains + 6), a3, w3, sum, corners);
   }
   const SV<float> a0 = base_solve(M, sum.I, sum.p, B);
   if (PEEL) {
@@ -152,8 +152,9 @@ __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>
 // One warp: theta th13 against windows [32 wb, 32 wb + 32) of win, writing the partials of the
 // four eight-window groups g = 4 wb .. 4 wb + 3 (those below G) to partial_n[g][SPI_N_COMP].
 // lane_smem: the CTA's lane_smem_bytes<PEEL>() of dynamic shared memory; bp_warp / gains_warp: the
-// CTA's per-warp parameter slots. Callable repeatedly by one warp (persistent kernels).
-template <bool PEEL>
+// CTA's per-warp parameter slots. MS: the motor shape (motor_shape_of the model, or
+// kMotorRuntime). Callable repeatedly by one warp (persistent kernels).
+template <bool PEEL, int MS = kMotorRuntime>
 __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinView& win, const float* th13, int wb,
                                                   float* partial_n, int G, unsigned long long* n_bad,
                                                   float4* lane_smem, BaseParams<float>* bp_warp,
@@ -196,7 +197,7 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
   for (int h = 0; h < H; ++h) {
     const float4* ap = reinterpret_cast<const float4*>(win.act + ((size_t)h * W + w) * 12);
     sl.put_targets<PEEL>(M, __ldg(ap), __ldg(ap + 1), __ldg(ap + 2));
-    for (int s = 0; s < dec; ++s) substep_lane<PEEL>(M, B, sl, &bp_warp[wib], gains_warp[wib]);
+    for (int s = 0; s < dec; ++s) substep_lane<PEEL, MS>(M, B, sl, &bp_warp[wib], gains_warp[wib]);
   }
   LegState<float> L[4];
 #pragma unroll
@@ -237,7 +238,7 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
 // One warp per (theta n, block of 32 windows); grid covers N * ceil(W / 32) warps; G is the
 // number of eight-window groups (ceil(W / 8)) of the partial layout. CTAs of 128 threads with
 // lane_smem_bytes<(MINB >= 4)>() of dynamic shared memory.
-template <int MINB>
+template <int MINB, int MS = kMotorRuntime>
 __global__ void __launch_bounds__(128, MINB) rollout_lane_kernel(const __grid_constant__ DevModel M, WinView win,
                                                                  const float* __restrict__ theta, int N, int G,
                                                                  float* __restrict__ partial,
@@ -249,7 +250,7 @@ __global__ void __launch_bounds__(128, MINB) rollout_lane_kernel(const __grid_co
   const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (warp >= (long long)N * WB) return;   // uniform per warp
   const int n = (int)(warp / WB), wb = (int)(warp % WB);
-  rollout_lane_warp<(MINB >= 4)>(M, win, theta + (size_t)n * SPI_THETA_DIM, wb, partial + (size_t)n * G * SPI_N_COMP,
+  rollout_lane_warp<(MINB >= 4), MS>(M, win, theta + (size_t)n * SPI_THETA_DIM, wb, partial + (size_t)n * G * SPI_N_COMP,
                                  G, n_bad, lane_smem, bp_warp, gains_warp);
 }
 

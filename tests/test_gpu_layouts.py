@@ -74,6 +74,34 @@ def test_layout_ragged_sizes(built, W, H, N, variant):
     assert cost_error(comp.cpu().numpy(), _oracle_comp(init, actions, target, th)) <= 1e-4
 
 
+@pytest.mark.parametrize("kw", [dict(tanh_a=(15.0, 18.0, 25.0), hip_action_scale=0.5),
+                                dict(motor_gain=(0.9, 1.1, 1.05), torque_speed=False),
+                                dict(torque_speed=False)])
+def test_lane3_motor_models_match_oracle(built, kw):
+    """lane3 runs a kernel specialised to the default motor model (torque-speed limit, unit
+    gains, no tanh saturation) and the run-time-flag kernel for any other; each motor model
+    here takes the latter, against the FP64 oracle with the same settings, over H = 10."""
+    from spi_gb300.autotune import set_variant
+    from spi_gb300.engine import Engine
+    from spi_gb300.robot import SimConfig
+    sim = gm.SimParams(**{k: (np.asarray(v, dtype=np.float64) if isinstance(v, tuple) else v) for k, v in kw.items()})
+    rng = np.random.default_rng(202)
+    _, init, actions, target = oracle_windows(13, n_traj=2, T=40, H=10, sim=sim)
+    init, actions, target = init[:48], actions[:48], target[:48]
+    th = random_theta(rng, 16).astype(np.float32)
+    e = Engine(SimConfig(**kw))
+    e.load_windows(torch.from_numpy(init), torch.from_numpy(actions), torch.from_numpy(target))
+    set_variant(e, "lane3")
+    comp, cost = e.evaluate(torch.from_numpy(th))
+    assert e.sync() == 0
+    N, W = th.shape[0], init.shape[0]
+    ref = dyn.rollout(np.tile(init.astype(np.float64), (N, 1)), np.tile(actions.astype(np.float64), (N, 1, 1)),
+                      np.repeat(th.astype(np.float64), W, 0), sim)
+    refc = oc.window_components(ref, np.tile(target.astype(np.float64), (N, 1))).reshape(N, W, 9).mean(1)
+    assert cost_error(comp.cpu().numpy(), refc) <= 1e-4
+    assert cost_error(cost.cpu().numpy(), oc.scalar_cost(refc)) <= 1e-4
+
+
 def test_layouts_agree(built):
     rng = np.random.default_rng(201)
     _, init, actions, target = oracle_windows(12, n_traj=4, T=60, H=10)
