@@ -274,14 +274,6 @@ template <int AX, class T> SPI_INL SV<T> ri_col(const RI<T>& a) {
 }
 // Articulated-inertia form [[I, [h]x], [[h]x^T, m 1]].
 template <class T> SPI_INL Art<T> ri_art(const RI<T>& a) { return rigid(a.m, a.h, a.I); }
-// I += ri_art(a), its structural zeros not added.
-template <class T> SPI_INL void ri_art_add(Art<T>& I, const RI<T>& a) {
-  I.A.xx += a.I.xx; I.A.yy += a.I.yy; I.A.zz += a.I.zz; I.A.xy += a.I.xy; I.A.xz += a.I.xz; I.A.yz += a.I.yz;
-  I.B.m[0][1] -= a.h.z; I.B.m[0][2] += a.h.y;
-  I.B.m[1][0] += a.h.z; I.B.m[1][2] -= a.h.x;
-  I.B.m[2][0] -= a.h.y; I.B.m[2][1] += a.h.x;
-  I.C.xx += a.m; I.C.yy += a.m; I.C.zz += a.m;
-}
 
 // Joint-origin sparsity. RM = 2: origin on the y axis (thigh joints), RM = 4: on the z axis
 // (calf joints), RM = 7: general (hip joints). The model builder checks the pattern.
@@ -423,17 +415,36 @@ template <int AX, int RM, class T> SPI_INL RI<T> ri_to_parent(const RI<T>& c, T 
     o.I.xy = I1.xy - a.x * y; o.I.xz = I1.xz; o.I.yz = I1.yz - a.z * y;
     return o;
   }
-  const V3<T> mr = c.m * r;
-  o.h = a + mr;
-  const T ax = a.x * r.x, ay = a.y * r.y, az = a.z * r.z;
-  const T qx = mr.x * r.x, qy = mr.y * r.y, qz = mr.z * r.z;
-  o.I.xx = I1.xx + T(2) * (ay + az) + (qy + qz);
-  o.I.yy = I1.yy + T(2) * (ax + az) + (qx + qz);
-  o.I.zz = I1.zz + T(2) * (ax + ay) + (qx + qy);
-  o.I.xy = I1.xy - (a.x * r.y + a.y * r.x) - mr.x * r.y;
-  o.I.xz = I1.xz - (a.x * r.z + a.z * r.x) - mr.x * r.z;
-  o.I.yz = I1.yz - (a.y * r.z + a.z * r.y) - mr.y * r.z;
+  // with h' = a + m r and u = a + h' = 2 a + m r: I'.xx = I1.xx + u.y r.y + u.z r.z (and cyclic),
+  // I'.xy = I1.xy - h'.x r.y - a.y r.x (and the like), two multiply-adds an entry
+  o.h = v3(a.x + c.m * r.x, a.y + c.m * r.y, a.z + c.m * r.z);
+  const V3<T> u = a + o.h;
+  o.I.xx = I1.xx + u.y * r.y + u.z * r.z;
+  o.I.yy = I1.yy + u.x * r.x + u.z * r.z;
+  o.I.zz = I1.zz + u.x * r.x + u.y * r.y;
+  o.I.xy = I1.xy - o.h.x * r.y - a.y * r.x;
+  o.I.xz = I1.xz - o.h.x * r.z - a.z * r.x;
+  o.I.yz = I1.yz - o.h.y * r.z - a.z * r.y;
   return o;
+}
+
+// acc += ri_art(ri_to_parent<AX, 7>(c, cs, sn, r)) (general joint origin r): the rotated
+// inertia accumulates straight onto acc's rotational block.
+template <int AX, class T> SPI_INL void ri_to_parent_art_acc(const RI<T>& c, T cs, T sn, V3<T> r, Art<T>& acc) {
+  const S3<T> I1 = rot_sym_acc<AX>(cs, sn, c.I, acc.A);
+  const V3<T> a = rot<AX>(cs, sn, c.h);
+  const V3<T> h = v3(a.x + c.m * r.x, a.y + c.m * r.y, a.z + c.m * r.z);
+  const V3<T> u = a + h;
+  acc.A.xx = I1.xx + u.y * r.y + u.z * r.z;
+  acc.A.yy = I1.yy + u.x * r.x + u.z * r.z;
+  acc.A.zz = I1.zz + u.x * r.x + u.y * r.y;
+  acc.A.xy = I1.xy - h.x * r.y - a.y * r.x;
+  acc.A.xz = I1.xz - h.x * r.z - a.z * r.x;
+  acc.A.yz = I1.yz - h.y * r.z - a.z * r.y;
+  acc.B.m[0][1] -= h.z; acc.B.m[0][2] += h.y;
+  acc.B.m[1][0] += h.z; acc.B.m[1][2] -= h.x;
+  acc.B.m[2][0] -= h.y; acc.B.m[2][1] += h.x;
+  acc.C.xx += c.m; acc.C.yy += c.m; acc.C.zz += c.m;
 }
 
 // ---------------------------------------------------------------------------
@@ -791,7 +802,7 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   W.put_col(1, Kp1, y1, l20);
   W.put_col(2, Kp2, y2, l21);
   // the leg at the base: articulated inertia I_c - K D^-1 K^T, bias p_c + K y
-  if (ACC) ri_art_add(out.I, ri_to_parent<0, 7>(Rc0, C[0], S[0], r0));
+  if (ACC) ri_to_parent_art_acc<0>(Rc0, C[0], S[0], r0, out.I);
   else out.I = ri_art(ri_to_parent<0, 7>(Rc0, C[0], S[0], r0));
   art_sub_outer(out.I, Kp0, K0);
   art_sub_outer(out.I, Kp1, K1);

@@ -123,8 +123,8 @@ __global__ void __launch_bounds__(128, MINB) server_rollout_kernel(const DevMode
 
 // The same in the lane layout: each work item is one (slot, theta, 32-window block), one lane
 // per window through all four legs (rollout_lane_warp). CTAs of 128 threads with kLaneParkBytes
-// of dynamic shared memory; the model by value.
-template <int MINB>
+// of dynamic shared memory; the model by value; MS its motor shape.
+template <int MINB, int MS = kMotorRuntime>
 __global__ void __launch_bounds__(128, MINB) server_rollout_lane_kernel(const __grid_constant__ DevModel M,
                                                                   const SlotDesc* __restrict__ slots,
                                                                   const int* __restrict__ order_all,
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(128, MINB) server_rollout_lane_kernel(const __
       const long long local = item - begin[order[lo]];
       const int WB = (S.win.W + 31) >> 5;
       const int n = (int)(local / WB), wb = (int)(local % WB);
-      rollout_lane_warp<false>(M, S.win, S.theta + (size_t)n * SPI_THETA_DIM, wb,
+      rollout_lane_warp<false, MS>(M, S.win, S.theta + (size_t)n * SPI_THETA_DIM, wb,
                                S.partial + (size_t)n * S.G * SPI_N_COMP, S.G, n_bad, lane_smem, bp_warp, gains_warp);
     }
   }
@@ -282,6 +282,9 @@ int enqueue_tick(spi_server* s) {
     if (s->layout == SPI_LAYOUT_LANE) {
       if (s->min_blocks <= 2)
         server_rollout_lane_kernel<2><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
+            s->host_model, s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
+      else if (motor_shape_of(s->host_model) == kMotorSpeedLimit)
+        server_rollout_lane_kernel<3, kMotorSpeedLimit><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
             s->host_model, s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
       else
         server_rollout_lane_kernel<3><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
@@ -468,6 +471,9 @@ int spi_server_set_kernel_layout(spi_server* s, int layout) {
     if (ce == cudaSuccess)
       ce = cudaFuncSetAttribute(server_rollout_lane_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 kLaneParkBytes);
+    if (ce == cudaSuccess)
+      ce = cudaFuncSetAttribute(server_rollout_lane_kernel<3, kMotorSpeedLimit>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, kLaneParkBytes);
     if (ce != cudaSuccess) return cuda_error(ce, "spi_server_set_kernel_layout: shared-memory attribute");
     s->min_blocks = std::min(std::max(s->min_blocks, 2), 3);
   } else {
