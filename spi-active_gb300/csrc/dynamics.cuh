@@ -587,6 +587,24 @@ template <class T> SPI_INL V3<T> contact_force(const DevModel& M, T radius, T z,
   return v3(-scale * v.x, -scale * v.y, fn);
 }
 
+// contact_force evaluated in the frame of the contact point's body: n is the world vertical
+// there (unit), v the point's velocity there. The tangential velocity is v - (n.v) n, whose norm
+// is the world-horizontal speed; returns the force in that frame with the implicit point mass's
+// share of the gravity shift (mimp g along n) included.
+template <class T> SPI_INL V3<T> contact_force_local(const DevModel& M, T radius, T z, V3<T> v, V3<T> n, T* mimp) {
+  const T vz = dot(n, v);
+  const V3<T> vt = v3(v.x - vz * n.x, v.y - vz * n.y, v.z - vz * n.z);
+  T pen = radius - z;
+  T s = m_clamp(pen * T(M.ramp_inv), T(0), T(1));
+  T fn = m_sel(pen > T(0), m_fmax(T(0), T(M.k) * pen - T(M.c) * s * vz), T(0));
+  T vtn = m_sqrt(dot(vt, vt));
+  T lim = T(M.mu) * fn;
+  T scale = m_sel(T(M.ct) * vtn <= lim, T(M.ct), lim / vtn);
+  *mimp = m_mul2_c(s, M.dt, M.imp_c, M.dt_imp_c);
+  const T fz = fn + *mimp * T(M.g);
+  return v3(fz * n.x - scale * vt.x, fz * n.y - scale * vt.y, fz * n.z - scale * vt.z);
+}
+
 // Spatial inertia of a point mass m at r added to I.
 template <class T> SPI_INL void add_point_mass(Art<T>& I, T m, V3<T> r) {
   const V3<T> h = m * r;
@@ -732,25 +750,19 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   SV<T> v2 = motion_to_child<1, 4>(v1, C[2], S[2], r2);   v2.w.y = v2.w.y + L.qd[2];
   const SV<T> cb0 = vel_product<0>(v0, L.qd[0]), cb1 = vel_product<1>(v1, L.qd[1]),
               cb2 = vel_product<1>(v2, L.qd[2]);
-  // foot: position and velocity, calf -> thigh -> hip -> base -> world
-  V3<T> fc = v3(T(M.foot[0]), T(M.foot[1]), T(M.foot[2]));
-  V3<T> vf = cross_acc(v2.w, fc, v2.v);
-  V3<T> pf = rot_acc<1>(C[2], S[2], fc, r2);
-  vf = rot<1>(C[2], S[2], vf);
-  pf = rot_acc<1>(C[1], S[1], pf, r1);
-  vf = rot<1>(C[1], S[1], vf);
-  pf = rot_acc<0>(C[0], S[0], pf, r0);
-  vf = rot<0>(C[0], S[0], vf);
+  // foot contact, evaluated in the calf frame: the world vertical brought down the chain (g_k in
+  // body k's parent frame), the foot height from it and the joint origins, the foot velocity
+  // from the calf's. The implicit point mass acts on the true acceleration while the dynamics
+  // run in the gravity-shifted frame: its share of the shift enters as a force mimp g upwards.
+  const V3<T> fc = v3(T(M.foot[0]), T(M.foot[1]), T(M.foot[2]));
+  const V3<T> g0 = row(B.R, 2);
+  const V3<T> g1 = rotT<0>(C[0], S[0], g0);
+  const V3<T> g2 = rotT<1>(C[1], S[1], g1);
+  const V3<T> g3 = rotT<1>(C[2], S[2], g2);
+  const T zf = B.p.z + g0.x * r0.x + g0.y * r0.y + g0.z * r0.z + g1.y * r1.y + g2.z * r2.z + g3.x * fc.x +
+               g3.y * fc.y + g3.z * fc.z;
   T mimp;
-  V3<T> F = contact_force(M, T(M.foot_r),
-                          B.p.z + B.R.m[2][0] * pf.x + B.R.m[2][1] * pf.y + B.R.m[2][2] * pf.z, mul(B.R, vf), &mimp);
-  // the implicit point mass acts on the true acceleration while the dynamics run in the
-  // gravity-shifted frame: its share of the shift enters as a force mimp*g upwards
-  F.z = F.z + mimp * T(M.g);
-  V3<T> Fc = mulT(B.R, F);
-  Fc = rotT<0>(C[0], S[0], Fc);
-  Fc = rotT<1>(C[1], S[1], Fc);
-  Fc = rotT<1>(C[2], S[2], Fc);
+  const V3<T> Fc = contact_force_local(M, T(M.foot_r), zf, cross_acc(v2.w, fc, v2.v), g3, &mimp);
   // composite inertias: calf (+ the contact's implicit point mass at the foot) -> thigh -> hip
   const RI<T> Ical = lc_ri<T>(lc, 2);
   RI<T> Rc2 = Ical;
