@@ -276,22 +276,27 @@ template <int AX, class T> SPI_INL SV<T> ri_col(const RI<T>& a) {
 template <class T> SPI_INL Art<T> ri_art(const RI<T>& a) { return rigid(a.m, a.h, a.I); }
 
 // Joint-origin sparsity. RM = 2: origin on the y axis (thigh joints), RM = 4: on the z axis
-// (calf joints), RM = 7: general (hip joints). The model builder checks the pattern.
+// (calf joints), RM = 3: in the x-y plane (hip joints), RM = 7: general. The model builder
+// checks the pattern.
+constexpr int kHipRM = 3;
 // r x u for an origin r with zero components skipped.
 template <int RM, class T> SPI_INL V3<T> rcross(V3<T> r, V3<T> u) {
   if (RM == 2) return v3(r.y * u.z, T(0), -(r.y * u.x));
   if (RM == 4) return v3(-(r.z * u.y), r.z * u.x, T(0));
+  if (RM == 3) return v3(r.y * u.z, -(r.x * u.z), r.x * u.y - r.y * u.x);
   return cross(r, u);
 }
-// u - r x w, with the known-zero component of r x w not subtracted.
+// u - r x w, with the known-zero terms of r x w not subtracted.
 template <int RM, class T> SPI_INL V3<T> sub_rcross(V3<T> u, V3<T> r, V3<T> w) {
   if (RM == 2) return v3(u.x - r.y * w.z, u.y, u.z + r.y * w.x);
   if (RM == 4) return v3(u.x + r.z * w.y, u.y - r.z * w.x, u.z);
+  if (RM == 3) return v3(u.x - r.y * w.z, u.y + r.x * w.z, u.z - r.x * w.y + r.y * w.x);
   return v3(u.x - r.y * w.z + r.z * w.y, u.y - r.z * w.x + r.x * w.z, u.z - r.x * w.y + r.y * w.x);
 }
 template <int RM, class T> SPI_INL V3<T> add_rcross(V3<T> u, V3<T> r, V3<T> w) {
   if (RM == 2) return v3(u.x + r.y * w.z, u.y, u.z - r.y * w.x);
   if (RM == 4) return v3(u.x - r.z * w.y, u.y + r.z * w.x, u.z);
+  if (RM == 3) return v3(u.x + r.y * w.z, u.y - r.x * w.z, u.z + r.x * w.y - r.y * w.x);
   return v3(u.x + r.y * w.z - r.z * w.y, u.y + r.z * w.x - r.x * w.z, u.z + r.x * w.y - r.y * w.x);
 }
 // acc + R u for the active rotation about AX.
@@ -417,6 +422,17 @@ template <int AX, int RM, class T> SPI_INL RI<T> ri_to_parent(const RI<T>& c, T 
   }
   // with h' = a + m r and u = a + h' = 2 a + m r: I'.xx = I1.xx + u.y r.y + u.z r.z (and cyclic),
   // I'.xy = I1.xy - h'.x r.y - a.y r.x (and the like), two multiply-adds an entry
+  if (RM == 3) {   // r = (x, y, 0)
+    o.h = v3(a.x + c.m * r.x, a.y + c.m * r.y, a.z);
+    const T ux = a.x + o.h.x, uy = a.y + o.h.y;
+    o.I.xx = I1.xx + uy * r.y;
+    o.I.yy = I1.yy + ux * r.x;
+    o.I.zz = I1.zz + ux * r.x + uy * r.y;
+    o.I.xy = I1.xy - o.h.x * r.y - a.y * r.x;
+    o.I.xz = I1.xz - a.z * r.x;
+    o.I.yz = I1.yz - a.z * r.y;
+    return o;
+  }
   o.h = v3(a.x + c.m * r.x, a.y + c.m * r.y, a.z + c.m * r.z);
   const V3<T> u = a + o.h;
   o.I.xx = I1.xx + u.y * r.y + u.z * r.z;
@@ -428,19 +444,33 @@ template <int AX, int RM, class T> SPI_INL RI<T> ri_to_parent(const RI<T>& c, T 
   return o;
 }
 
-// acc += ri_art(ri_to_parent<AX, 7>(c, cs, sn, r)) (general joint origin r): the rotated
-// inertia accumulates straight onto acc's rotational block.
-template <int AX, class T> SPI_INL void ri_to_parent_art_acc(const RI<T>& c, T cs, T sn, V3<T> r, Art<T>& acc) {
+// acc += ri_art(ri_to_parent<AX, RM>(c, cs, sn, r)) for a joint origin r in the x-y plane
+// (RM = 3) or general (RM = 7): the rotated inertia accumulates straight onto acc's
+// rotational block.
+template <int AX, int RM, class T> SPI_INL void ri_to_parent_art_acc(const RI<T>& c, T cs, T sn, V3<T> r, Art<T>& acc) {
+  static_assert(RM == 3 || RM == 7, "ri_to_parent_art_acc: origin pattern");
   const S3<T> I1 = rot_sym_acc<AX>(cs, sn, c.I, acc.A);
   const V3<T> a = rot<AX>(cs, sn, c.h);
-  const V3<T> h = v3(a.x + c.m * r.x, a.y + c.m * r.y, a.z + c.m * r.z);
-  const V3<T> u = a + h;
-  acc.A.xx = I1.xx + u.y * r.y + u.z * r.z;
-  acc.A.yy = I1.yy + u.x * r.x + u.z * r.z;
-  acc.A.zz = I1.zz + u.x * r.x + u.y * r.y;
-  acc.A.xy = I1.xy - h.x * r.y - a.y * r.x;
-  acc.A.xz = I1.xz - h.x * r.z - a.z * r.x;
-  acc.A.yz = I1.yz - h.y * r.z - a.z * r.y;
+  V3<T> h;
+  if (RM == 3) {
+    h = v3(a.x + c.m * r.x, a.y + c.m * r.y, a.z);
+    const T ux = a.x + h.x, uy = a.y + h.y;
+    acc.A.xx = I1.xx + uy * r.y;
+    acc.A.yy = I1.yy + ux * r.x;
+    acc.A.zz = I1.zz + ux * r.x + uy * r.y;
+    acc.A.xy = I1.xy - h.x * r.y - a.y * r.x;
+    acc.A.xz = I1.xz - a.z * r.x;
+    acc.A.yz = I1.yz - a.z * r.y;
+  } else {
+    h = v3(a.x + c.m * r.x, a.y + c.m * r.y, a.z + c.m * r.z);
+    const V3<T> u = a + h;
+    acc.A.xx = I1.xx + u.y * r.y + u.z * r.z;
+    acc.A.yy = I1.yy + u.x * r.x + u.z * r.z;
+    acc.A.zz = I1.zz + u.x * r.x + u.y * r.y;
+    acc.A.xy = I1.xy - h.x * r.y - a.y * r.x;
+    acc.A.xz = I1.xz - h.x * r.z - a.z * r.x;
+    acc.A.yz = I1.yz - h.y * r.z - a.z * r.y;
+  }
   acc.B.m[0][1] -= h.z; acc.B.m[0][2] += h.y;
   acc.B.m[1][0] += h.z; acc.B.m[1][2] -= h.x;
   acc.B.m[2][0] -= h.y; acc.B.m[2][1] += h.x;
@@ -745,7 +775,7 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   const F4* lc = M.legc[leg];
   V3<T> r0 = lc_org<T>(lc, 0), r1 = lc_org<T>(lc, 1), r2 = lc_org<T>(lc, 2);
   // body velocities (body coordinates) and velocity-product accelerations
-  SV<T> v0 = motion_to_child<0>(B.nu, C[0], S[0], r0); v0.w.x = v0.w.x + L.qd[0];
+  SV<T> v0 = motion_to_child<0, kHipRM>(B.nu, C[0], S[0], r0); v0.w.x = v0.w.x + L.qd[0];
   SV<T> v1 = motion_to_child<1, 2>(v0, C[1], S[1], r1);   v1.w.y = v1.w.y + L.qd[1];
   SV<T> v2 = motion_to_child<1, 4>(v1, C[2], S[2], r2);   v2.w.y = v2.w.y + L.qd[2];
   const SV<T> cb0 = vel_product<0>(v0, L.qd[0]), cb1 = vel_product<1>(v1, L.qd[1]),
@@ -759,7 +789,7 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   const V3<T> g1 = rotT<0>(C[0], S[0], g0);
   const V3<T> g2 = rotT<1>(C[1], S[1], g1);
   const V3<T> g3 = rotT<1>(C[2], S[2], g2);
-  const T zf = B.p.z + g0.x * r0.x + g0.y * r0.y + g0.z * r0.z + g1.y * r1.y + g2.z * r2.z + g3.x * fc.x +
+  const T zf = B.p.z + g0.x * r0.x + g0.y * r0.y + g1.y * r1.y + g2.z * r2.z + g3.x * fc.x +
                g3.y * fc.y + g3.z * fc.z;
   T mimp;
   const V3<T> Fc = contact_force_local(M, T(M.foot_r), zf, cross_acc(v2.w, fc, v2.v), g3, &mimp);
@@ -786,7 +816,8 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
     const RI<T> Ihp = lc_ri<T>(lc, 0);
     f0 = ri_mul_acc(Ihp, cb0, crf_acc(v0, ri_mul(Ihp, v0), force_to_parent<1, 2>(f1, C[1], S[1], r1)));
   }
-  const SV<T> pc = ACC ? force_to_parent_acc<0, 7>(f0, C[0], S[0], r0, out.p) : force_to_parent<0, 7>(f0, C[0], S[0], r0);
+  const SV<T> pc = ACC ? force_to_parent_acc<0, kHipRM>(f0, C[0], S[0], r0, out.p)
+                       : force_to_parent<0, kHipRM>(f0, C[0], S[0], r0);
   // joint force columns F_k = I_k^c S_k in base coordinates, and the joint-space inertia
   const SV<T> F2t = force_to_parent<1, 4>(ri_col<1>(Rc2), C[2], S[2], r2);
   const SV<T> F2h = force_to_parent<1, 2>(F2t, C[1], S[1], r1);
@@ -802,9 +833,9 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   const T l21 = e12 * i1;
   const T i2 = T(1) / (M22 - l20 * M02 - l21 * e12);
   // K = F L^-T (base coordinates), K' = K D^-1, y = D^-1 L^-1 (tau - C)
-  const SV<T> K0 = force_to_parent<0, 7>(F0h, C[0], S[0], r0);
-  const SV<T> K1 = sub_scaled(force_to_parent<0, 7>(F1h, C[0], S[0], r0), l10, K0);
-  const SV<T> K2 = sub_scaled(sub_scaled(force_to_parent<0, 7>(F2h, C[0], S[0], r0), l20, K0), l21, K1);
+  const SV<T> K0 = force_to_parent<0, kHipRM>(F0h, C[0], S[0], r0);
+  const SV<T> K1 = sub_scaled(force_to_parent<0, kHipRM>(F1h, C[0], S[0], r0), l10, K0);
+  const SV<T> K2 = sub_scaled(sub_scaled(force_to_parent<0, kHipRM>(F2h, C[0], S[0], r0), l20, K0), l21, K1);
   const SV<T> Kp0 = i0 * K0, Kp1 = i1 * K1, Kp2 = i2 * K2;
   const T z0 = tau[0] - f0.w.x;
   const T z1 = (tau[1] - f1.w.y) - l10 * z0;
@@ -814,8 +845,8 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   W.put_col(1, Kp1, y1, l20);
   W.put_col(2, Kp2, y2, l21);
   // the leg at the base: articulated inertia I_c - K D^-1 K^T, bias p_c + K y
-  if (ACC) ri_to_parent_art_acc<0>(Rc0, C[0], S[0], r0, out.I);
-  else out.I = ri_art(ri_to_parent<0, 7>(Rc0, C[0], S[0], r0));
+  if (ACC) ri_to_parent_art_acc<0, kHipRM>(Rc0, C[0], S[0], r0, out.I);
+  else out.I = ri_art(ri_to_parent<0, kHipRM>(Rc0, C[0], S[0], r0));
   art_sub_outer(out.I, Kp0, K0);
   art_sub_outer(out.I, Kp1, K1);
   art_sub_outer(out.I, Kp2, K2);

@@ -33,7 +33,11 @@ inline int build_dev_model(const spi_robot& r, DevModel* M, const char** why) {
       lc[5 + 3 * k] = F4{r.body_I[b][4], r.body_I[b][5],
                          r.torque_speed ? (float)(1.0 / (double)r.velocity_limit[b]) : 0.0f, 0.0f};
       if (!(r.body_mass[b] > 0.0f)) { *why = "leg body mass must be > 0"; return SPI_EINVAL; }
-      // the kernel's transforms assume thigh joints offset along y and calf joints along z
+      // the kernel's transforms assume hip joints in the base's x-y plane, thigh joints offset
+      // along y and calf joints along z
+      if (k == 0 && r.body_origin[b][2] != 0.0f) {
+        *why = "hip joint origins must lie in the base frame's x-y plane"; return SPI_EINVAL;
+      }
       if (k == 1 && (r.body_origin[b][0] != 0.0f || r.body_origin[b][2] != 0.0f)) {
         *why = "thigh joint origins must lie on the hip frame's y axis"; return SPI_EINVAL;
       }

@@ -56,3 +56,28 @@ def test_kernel_variant_and_fisher_entry_points_validate_arguments(built):
     srv = _bind(ctypes.CDLL(lib._name))
     assert srv.spi_server_set_kernel_layout(None, 1) == -1
     assert srv.spi_server_set_kernel_config(None, 3) == -1
+
+
+def test_model_builder_rejects_unsupported_joint_origins(built):
+    """The kernel's transforms take hip joint origins in the base's x-y plane, thigh origins
+    on the hip frame's y axis and calf origins on the thigh frame's z axis; the model builder
+    (shared by the engine and the host emulation) refuses any other robot with SPI_EINVAL."""
+    import numpy as np
+    from spi_gb300 import _lib
+    from spi_gb300.data import standing_state
+    from spi_gb300.robot import SimConfig, THETA_NOMINAL, to_struct
+    lib = _lib.hostemu_lib()
+    x = np.ascontiguousarray(standing_state(1), dtype=np.float64)
+    th = np.ascontiguousarray(THETA_NOMINAL[None], dtype=np.float64)
+    a = np.zeros((1, 1, 12))
+    out = np.zeros((1, 1, 37))
+
+    def run(r):
+        return lib.spi_hostemu_rollout(ctypes.byref(r), x.ctypes.data, a.ctypes.data, th.ctypes.data, 1, 1,
+                                       out.ctypes.data)
+
+    assert run(to_struct(SimConfig())) == 0
+    for body, comp in ((0, 2), (1, 0), (7, 2), (2, 1), (11, 0)):   # body 3 leg + k: hip z, thigh x / z, calf y / x
+        r = to_struct(SimConfig())
+        r.body_origin[body][comp] = 0.01
+        assert run(r) == -1, (body, comp)
