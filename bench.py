@@ -429,7 +429,7 @@ def run_ours(args):
     peak = probe_fp32_peak()
     achieved = steps_per_iter * fl / (kmean * 1e-3)
     roof = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": 419840 if variant.startswith("lane") else 419328,
+            "frac": achieved / peak, "traffic": 418304 if variant.startswith("lane") else 419328,
             "traffic_note": "dram read+write bytes per launch from ncu on 1024 theta x the same 256 windows "
                             "(profiles/rollout_lane_kernel_1024x256xH20.md, rollout_kernel_1024x256xH20_full.md); "
                             "the window set is read once and theta / partials stay in L2, so traffic does not "
