@@ -738,6 +738,82 @@ template <class T> SPI_INL void art_sub_outer(Art<T>& I, const SV<T>& a, const S
   I.C.xy -= a.v.x * b.v.y; I.C.xz -= a.v.x * b.v.z; I.C.yz -= a.v.y * b.v.z;
 }
 
+// Sparse forms of the above for operands with structural zeros. IEEE rules keep a product
+// with a literal 0.0f (it is NaN for an infinite factor), so these write only the terms that
+// are not structurally zero; for finite operands each equals its dense counterpart.
+//
+// acc + X m across a thigh joint (axis y, origin on y) for m = vel_product<0>(...) (m.w.x =
+// m.v.x = 0) and acc = vel_product<1>(...) (acc.w.y = acc.v.y = 0).
+template <class T> SPI_INL SV<T> thigh_accel(const SV<T>& m, T c, T s, V3<T> r, const SV<T>& acc) {
+  SV<T> o;
+  o.w = v3(acc.w.x - s * m.w.z, m.w.y, acc.w.z + c * m.w.z);
+  const T t = -(r.y * m.w.z);
+  o.v = v3(acc.v.x + c * t - s * m.v.z, m.v.y, acc.v.z + s * t + c * m.v.z);
+  return o;
+}
+// acc + X m across a joint about y (origin sparsity RM) for acc = vel_product<1>(...).
+template <int RM, class T> SPI_INL SV<T> motion_to_child_acc_y0(const SV<T>& m, T c, T s, V3<T> r, const SV<T>& acc) {
+  SV<T> o;
+  o.w = v3(acc.w.x + c * m.w.x - s * m.w.z, m.w.y, acc.w.z + s * m.w.x + c * m.w.z);
+  const V3<T> u = sub_rcross<RM>(m.v, r, m.w);
+  o.v = v3(acc.v.x + c * u.x - s * u.z, u.y, acc.v.z + s * u.x + c * u.z);
+  return o;
+}
+// acc + I m for m = vel_product<0>(...) (m.w.x = m.v.x = 0).
+template <class T> SPI_INL SV<T> ri_mul_acc_x0(const RI<T>& I, const SV<T>& m, const SV<T>& acc) {
+  const T a = m.w.y, b = m.w.z, c = m.v.y, d = m.v.z;
+  const V3<T> h = I.h;
+  SV<T> r;
+  r.w = v3(acc.w.x + I.I.xy * a + I.I.xz * b + h.y * d - h.z * c,
+           acc.w.y + I.I.yy * a + I.I.yz * b - h.x * d,
+           acc.w.z + I.I.yz * a + I.I.zz * b + h.x * c);
+  r.v = v3(acc.v.x + a * h.z - b * h.y, acc.v.y + I.m * c + b * h.x, acc.v.z + I.m * d - a * h.x);
+  return r;
+}
+// X^T f across a joint about y (origin sparsity RM = 2 or 4) for a joint force column
+// f = ri_col<1>(...) or one already carried across such a joint (f.v.y = 0, and so is the
+// result's).
+template <int RM, class T> SPI_INL SV<T> col_to_parent_y(const SV<T>& f, T c, T s, V3<T> r) {
+  SV<T> o;
+  o.v = v3(c * f.v.x + s * f.v.z, T(0), c * f.v.z - s * f.v.x);
+  const V3<T> u = rot<1>(c, s, f.w);
+  if (RM == 4) o.w = v3(u.x, u.y + r.z * o.v.x, u.z);
+  else o.w = v3(u.x + r.y * o.v.z, u.y, u.z - r.y * o.v.x);
+  return o;
+}
+// X^T f across the hip joint (axis x, origin in the x-y plane) for f.v.y = 0.
+template <class T> SPI_INL SV<T> hip_col_to_base_vy0(const SV<T>& f, T c, T s, V3<T> r) {
+  SV<T> o;
+  o.v = v3(f.v.x, -(s * f.v.z), c * f.v.z);
+  o.w = add_rcross<kHipRM>(rot<0>(c, s, f.w), r, o.v);
+  return o;
+}
+// X^T f across the hip joint for the hip's own column f = ri_col<0>(...) (f.v.x = 0, and so
+// is the result's).
+template <class T> SPI_INL SV<T> hip_col_to_base_vx0(const SV<T>& f, T c, T s, V3<T> r) {
+  SV<T> o;
+  o.v = v3(T(0), c * f.v.y - s * f.v.z, s * f.v.y + c * f.v.z);
+  const V3<T> u = rot<0>(c, s, f.w);
+  o.w = v3(u.x + r.y * o.v.z, u.y - r.x * o.v.z, u.z + r.x * o.v.y);
+  return o;
+}
+// K - s J (as sub_scaled) for J.v.x = 0.
+template <class T> SPI_INL SV<T> sub_scaled_vx0(const SV<T>& K, T s, const SV<T>& J) {
+  SV<T> r;
+  r.w = K.w - s * J.w;
+  r.v = v3(K.v.x, K.v.y - s * J.v.y, K.v.z - s * J.v.z);
+  return r;
+}
+// I -= a b^T (as art_sub_outer) for a.v.x = b.v.x = 0.
+template <class T> SPI_INL void art_sub_outer_vx0(Art<T>& I, const SV<T>& a, const SV<T>& b) {
+  I.A.xx -= a.w.x * b.w.x; I.A.yy -= a.w.y * b.w.y; I.A.zz -= a.w.z * b.w.z;
+  I.A.xy -= a.w.x * b.w.y; I.A.xz -= a.w.x * b.w.z; I.A.yz -= a.w.y * b.w.z;
+  I.B.m[0][1] -= a.w.x * b.v.y; I.B.m[0][2] -= a.w.x * b.v.z;
+  I.B.m[1][1] -= a.w.y * b.v.y; I.B.m[1][2] -= a.w.y * b.v.z;
+  I.B.m[2][1] -= a.w.z * b.v.y; I.B.m[2][2] -= a.w.z * b.v.z;
+  I.C.yy -= a.v.y * b.v.y; I.C.zz -= a.v.z * b.v.z; I.C.yz -= a.v.y * b.v.z;
+}
+
 // ---------------------------------------------------------------------------
 // Phase A: everything of one leg (and two base corners) up to its base contribution.
 //
@@ -801,8 +877,8 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   const RI<T> Rc0 = ri_to_parent_acc<1, 2>(Rc1, C[1], S[1], r1, lc_ri<T>(lc, 0));
   // bias pass (a0 = 0, qdd = 0): accelerations are the accumulated velocity products; the
   // implicit point mass takes part in the inertial force, not in the velocity term
-  const SV<T> ab1 = motion_to_child_acc<1, 2>(cb0, C[1], S[1], r1, cb1);
-  const SV<T> ab2 = motion_to_child_acc<1, 4>(ab1, C[2], S[2], r2, cb2);
+  const SV<T> ab1 = thigh_accel(cb0, C[1], S[1], r1, cb1);
+  const SV<T> ab2 = motion_to_child_acc_y0<4>(ab1, C[2], S[2], r2, cb2);
   SV<T> f2 = ri_mul_acc(Rc2, ab2, crf(v2, ri_mul(Ical, v2)));
   f2.w = cross_acc(Fc, fc, f2.w);
   f2.v = f2.v - Fc;
@@ -814,14 +890,14 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   SV<T> f0;
   {
     const RI<T> Ihp = lc_ri<T>(lc, 0);
-    f0 = ri_mul_acc(Ihp, cb0, crf_acc(v0, ri_mul(Ihp, v0), force_to_parent<1, 2>(f1, C[1], S[1], r1)));
+    f0 = ri_mul_acc_x0(Ihp, cb0, crf_acc(v0, ri_mul(Ihp, v0), force_to_parent<1, 2>(f1, C[1], S[1], r1)));
   }
   const SV<T> pc = ACC ? force_to_parent_acc<0, kHipRM>(f0, C[0], S[0], r0, out.p)
                        : force_to_parent<0, kHipRM>(f0, C[0], S[0], r0);
   // joint force columns F_k = I_k^c S_k in base coordinates, and the joint-space inertia
-  const SV<T> F2t = force_to_parent<1, 4>(ri_col<1>(Rc2), C[2], S[2], r2);
-  const SV<T> F2h = force_to_parent<1, 2>(F2t, C[1], S[1], r1);
-  const SV<T> F1h = force_to_parent<1, 2>(ri_col<1>(Rc1), C[1], S[1], r1);
+  const SV<T> F2t = col_to_parent_y<4>(ri_col<1>(Rc2), C[2], S[2], r2);
+  const SV<T> F2h = col_to_parent_y<2>(F2t, C[1], S[1], r1);
+  const SV<T> F1h = col_to_parent_y<2>(ri_col<1>(Rc1), C[1], S[1], r1);
   const SV<T> F0h = ri_col<0>(Rc0);
   const T M00 = Rc0.I.xx + P.arm, M11 = Rc1.I.yy + P.arm, M22 = Rc2.I.yy + P.arm;
   const T M01 = F1h.w.x, M02 = F2h.w.x, M12 = F2t.w.y;
@@ -833,10 +909,14 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   const T l21 = e12 * i1;
   const T i2 = T(1) / (M22 - l20 * M02 - l21 * e12);
   // K = F L^-T (base coordinates), K' = K D^-1, y = D^-1 L^-1 (tau - C)
-  const SV<T> K0 = force_to_parent<0, kHipRM>(F0h, C[0], S[0], r0);
-  const SV<T> K1 = sub_scaled(force_to_parent<0, kHipRM>(F1h, C[0], S[0], r0), l10, K0);
-  const SV<T> K2 = sub_scaled(sub_scaled(force_to_parent<0, kHipRM>(F2h, C[0], S[0], r0), l20, K0), l21, K1);
-  const SV<T> Kp0 = i0 * K0, Kp1 = i1 * K1, Kp2 = i2 * K2;
+  // (F0h.v.x = 0 and F1h.v.y = F2h.v.y = 0 by construction, so K0.v.x = 0)
+  const SV<T> K0 = hip_col_to_base_vx0(F0h, C[0], S[0], r0);
+  const SV<T> K1 = sub_scaled_vx0(hip_col_to_base_vy0(F1h, C[0], S[0], r0), l10, K0);
+  const SV<T> K2 = sub_scaled(sub_scaled_vx0(hip_col_to_base_vy0(F2h, C[0], S[0], r0), l20, K0), l21, K1);
+  SV<T> Kp0;
+  Kp0.w = i0 * K0.w;
+  Kp0.v = v3(T(0), i0 * K0.v.y, i0 * K0.v.z);
+  const SV<T> Kp1 = i1 * K1, Kp2 = i2 * K2;
   const T z0 = tau[0] - f0.w.x;
   const T z1 = (tau[1] - f1.w.y) - l10 * z0;
   const T z2 = (tau[2] - f2.w.y) - l20 * z0 - l21 * z1;
@@ -847,12 +927,12 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   // the leg at the base: articulated inertia I_c - K D^-1 K^T, bias p_c + K y
   if (ACC) ri_to_parent_art_acc<0, kHipRM>(Rc0, C[0], S[0], r0, out.I);
   else out.I = ri_art(ri_to_parent<0, kHipRM>(Rc0, C[0], S[0], r0));
-  art_sub_outer(out.I, Kp0, K0);
+  art_sub_outer_vx0(out.I, Kp0, K0);
   art_sub_outer(out.I, Kp1, K1);
   art_sub_outer(out.I, Kp2, K2);
   out.p.w = v3(pc.w.x + y2 * K2.w.x + y1 * K1.w.x + y0 * K0.w.x, pc.w.y + y2 * K2.w.y + y1 * K1.w.y + y0 * K0.w.y,
                pc.w.z + y2 * K2.w.z + y1 * K1.w.z + y0 * K0.w.z);
-  out.p.v = v3(pc.v.x + y2 * K2.v.x + y1 * K1.v.x + y0 * K0.v.x, pc.v.y + y2 * K2.v.y + y1 * K1.v.y + y0 * K0.v.y,
+  out.p.v = v3(pc.v.x + y2 * K2.v.x + y1 * K1.v.x, pc.v.y + y2 * K2.v.y + y1 * K1.v.y + y0 * K0.v.y,
                pc.v.z + y2 * K2.v.z + y1 * K1.v.z + y0 * K0.v.z);
   // two of the eight base-box corners, when corners_may_touch (a corner off the ground adds
   // exactly zero force and zero implicit mass)
@@ -988,8 +1068,9 @@ SPI_INL void phase_c(const DevModel& M, int leg, const SV<T>& a0, const WK& W, L
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const SV<T>& q = W.Kp[k];
-    w[k] = W.y[k] - q.w.x * a0.w.x - q.w.y * a0.w.y - q.w.z * a0.w.z - q.v.x * a0.v.x - q.v.y * a0.v.y -
-           q.v.z * a0.v.z;
+    // K'_0.v.x is 0 by construction (the hip's own force column has no x force)
+    const T vx = k == 0 ? W.y[k] : W.y[k] - q.v.x * a0.v.x;
+    w[k] = vx - q.w.x * a0.w.x - q.w.y * a0.w.y - q.w.z * a0.w.z - q.v.y * a0.v.y - q.v.z * a0.v.z;
   }
   const T w0 = w[0], w1 = w[1], w2 = w[2];
   T qdd[3];
