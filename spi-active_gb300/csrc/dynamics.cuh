@@ -253,14 +253,6 @@ template <class T> SPI_INL void ri_add(RI<T>& a, const RI<T>& b) {
   a.h = a.h + b.h;
   a.I.xx += b.I.xx; a.I.yy += b.I.yy; a.I.zz += b.I.zz; a.I.xy += b.I.xy; a.I.xz += b.I.xz; a.I.yz += b.I.yz;
 }
-// Adds a point mass mp at p.
-template <class T> SPI_INL void ri_add_point(RI<T>& a, T mp, V3<T> p) {
-  const V3<T> hp = mp * p;
-  a.m = a.m + mp;
-  a.h = a.h + hp;
-  a.I.xx += hp.y * p.y + hp.z * p.z; a.I.yy += hp.x * p.x + hp.z * p.z; a.I.zz += hp.x * p.x + hp.y * p.y;
-  a.I.xy -= hp.x * p.y; a.I.xz -= hp.x * p.z; a.I.yz -= hp.y * p.z;
-}
 template <class T> SPI_INL SV<T> ri_mul(const RI<T>& a, const SV<T>& v) { return rigid_mul(a.m, a.h, a.I, v); }
 template <class T> SPI_INL SV<T> ri_mul_acc(const RI<T>& a, const SV<T>& v, const SV<T>& acc) {
   return rigid_mul_acc(a.m, a.h, a.I, v, acc);
@@ -860,19 +852,26 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   // body k's parent frame), the foot height from it and the joint origins, the foot velocity
   // from the calf's. The implicit point mass acts on the true acceleration while the dynamics
   // run in the gravity-shifted frame: its share of the shift enters as a force mimp g upwards.
-  const V3<T> fc = v3(T(M.foot[0]), T(M.foot[1]), T(M.foot[2]));
+  // (the foot lies on the calf's z axis, fc = (0, 0, fz): the model builder checks it)
+  const T fz = T(M.foot[2]);
   const V3<T> g0 = row(B.R, 2);
   const V3<T> g1 = rotT<0>(C[0], S[0], g0);
   const V3<T> g2 = rotT<1>(C[1], S[1], g1);
   const V3<T> g3 = rotT<1>(C[2], S[2], g2);
-  const T zf = B.p.z + g0.x * r0.x + g0.y * r0.y + g1.y * r1.y + g2.z * r2.z + g3.x * fc.x +
-               g3.y * fc.y + g3.z * fc.z;
+  const T zf = B.p.z + g0.x * r0.x + g0.y * r0.y + g1.y * r1.y + g2.z * r2.z + g3.z * fz;
   T mimp;
-  const V3<T> Fc = contact_force_local(M, T(M.foot_r), zf, cross_acc(v2.w, fc, v2.v), g3, &mimp);
+  const V3<T> Fc = contact_force_local(M, T(M.foot_r), zf, v3(v2.v.x + v2.w.y * fz, v2.v.y - v2.w.x * fz, v2.v.z),
+                                       g3, &mimp);
   // composite inertias: calf (+ the contact's implicit point mass at the foot) -> thigh -> hip
   const RI<T> Ical = lc_ri<T>(lc, 2);
   RI<T> Rc2 = Ical;
-  ri_add_point(Rc2, mimp, fc);
+  {   // ri_add_point(Rc2, mimp, (0, 0, fz))
+    const T hz = mimp * fz, q = hz * fz;
+    Rc2.m = Rc2.m + mimp;
+    Rc2.h.z = Rc2.h.z + hz;
+    Rc2.I.xx = Rc2.I.xx + q;
+    Rc2.I.yy = Rc2.I.yy + q;
+  }
   const RI<T> Rc1 = ri_to_parent_acc<1, 4>(Rc2, C[2], S[2], r2, lc_ri<T>(lc, 1));
   const RI<T> Rc0 = ri_to_parent_acc<1, 2>(Rc1, C[1], S[1], r1, lc_ri<T>(lc, 0));
   // bias pass (a0 = 0, qdd = 0): accelerations are the accumulated velocity products; the
@@ -880,7 +879,7 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   const SV<T> ab1 = thigh_accel(cb0, C[1], S[1], r1, cb1);
   const SV<T> ab2 = motion_to_child_acc_y0<4>(ab1, C[2], S[2], r2, cb2);
   SV<T> f2 = ri_mul_acc(Rc2, ab2, crf(v2, ri_mul(Ical, v2)));
-  f2.w = cross_acc(Fc, fc, f2.w);
+  f2.w = v3(f2.w.x + Fc.y * fz, f2.w.y - Fc.x * fz, f2.w.z);   // + Fc x (0, 0, fz)
   f2.v = f2.v - Fc;
   SV<T> f1;
   {

@@ -64,6 +64,7 @@ inline int build_dev_model(const spi_robot& r, DevModel* M, const char** why) {
   }
   M->corner_reach *= 1.001f;   // margin over float rounding of the corner coordinates
   memcpy(M->foot, r.foot, sizeof(M->foot));
+  if (r.foot[0] != 0.0f || r.foot[1] != 0.0f) { *why = "the foot must lie on the calf frame's z axis"; return SPI_EINVAL; }
   memcpy(M->gain, r.motor_gain, sizeof(M->gain));
   memcpy(M->tanh_a, r.tanh_a, sizeof(M->tanh_a));
   memcpy(M->base_com, r.base_com, sizeof(M->base_com));

@@ -60,8 +60,9 @@ def test_kernel_variant_and_fisher_entry_points_validate_arguments(built):
 
 def test_model_builder_rejects_unsupported_joint_origins(built):
     """The kernel's transforms take hip joint origins in the base's x-y plane, thigh origins
-    on the hip frame's y axis and calf origins on the thigh frame's z axis; the model builder
-    (shared by the engine and the host emulation) refuses any other robot with SPI_EINVAL."""
+    on the hip frame's y axis, calf origins and the foot on the thigh's and the calf's z axes;
+    the model builder (shared by the engine and the host emulation) refuses any other robot
+    with SPI_EINVAL."""
     import numpy as np
     from spi_gb300 import _lib
     from spi_gb300.data import standing_state
@@ -81,3 +82,7 @@ def test_model_builder_rejects_unsupported_joint_origins(built):
         r = to_struct(SimConfig())
         r.body_origin[body][comp] = 0.01
         assert run(r) == -1, (body, comp)
+    for comp in (0, 1):                                              # the foot off the calf's z axis
+        r = to_struct(SimConfig())
+        r.foot[comp] = 0.01
+        assert run(r) == -1, comp

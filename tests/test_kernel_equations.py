@@ -19,7 +19,7 @@ from helpers import random_theta
 # roofline's algorithmic figure, and the kernel's condensed formulation (csrc/dynamics.cuh; the
 # joint targets of the actions are formed once per control step, outside the substep).
 FLOPS_PER_SUBSTEP = 7053
-EXECUTED_FLOPS_PER_SUBSTEP = 5305
+EXECUTED_FLOPS_PER_SUBSTEP = 5149
 
 
 def _emu(built, cfg, x0, acts, th):
