@@ -157,31 +157,48 @@ static __global__ void __launch_bounds__(1024) cem_refit_kernel(CemState* __rest
     if (lane == 0) { s_cov[i * CEM_MAX_DIM + j] = s / ne; s_cov[j * CEM_MAX_DIM + i] = s / ne; }
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    const double a = st->alpha;
-    for (int i = 0; i < P; ++i) st->mu[i] = a * s_mu[i] + (1.0 - a) * st->mu[i];
-    for (int i = 0; i < P; ++i)
-      for (int j = 0; j < P; ++j) {
-        double v = a * s_cov[i * CEM_MAX_DIM + j] + (1.0 - a) * st->cov[i * CEM_MAX_DIM + j];
-        if (i == j) v += st->min_std[i] * st->min_std[i];
-        st->cov[i * CEM_MAX_DIM + j] = v;
-      }
-    // Cholesky, lower
-    int ok = 1;
+  // smoothed mean and covariance (+ the std floor on the diagonal), element-parallel, kept in
+  // shared memory for the factorisation and written out once
+  __shared__ double s_L[CEM_MAX_DIM * CEM_MAX_DIM];
+  __shared__ int s_ok;
+  const double a = st->alpha;
+  if (threadIdx.x == 0) s_ok = 1;
+  for (int i = threadIdx.x; i < P; i += blockDim.x) st->mu[i] = a * s_mu[i] + (1.0 - a) * st->mu[i];
+  for (int q = threadIdx.x; q < P * P; q += blockDim.x) {
+    const int i = q / P, j = q % P;
+    double v = a * s_cov[i * CEM_MAX_DIM + j] + (1.0 - a) * st->cov[i * CEM_MAX_DIM + j];
+    if (i == j) v += st->min_std[i] * st->min_std[i];
+    s_cov[i * CEM_MAX_DIM + j] = v;
+    st->cov[i * CEM_MAX_DIM + j] = v;
+  }
+  __syncthreads();
+  // Cholesky, lower, by one warp: column j's diagonal on lane 0, then its rows i > j on lanes
+  // (each entry's sum in the serial order k = 0 .. j - 1)
+  if (warp == 0) {
     for (int j = 0; j < P; ++j) {
-      double d = st->cov[j * CEM_MAX_DIM + j];
-      for (int k = 0; k < j; ++k) d -= st->L[j * CEM_MAX_DIM + k] * st->L[j * CEM_MAX_DIM + k];
-      if (!(d > 0.0)) { ok = 0; d = st->min_std[j] * st->min_std[j]; }
-      const double ljj = sqrt(d);
-      st->L[j * CEM_MAX_DIM + j] = ljj;
-      for (int i = j + 1; i < P; ++i) {
-        double s = st->cov[i * CEM_MAX_DIM + j];
-        for (int k = 0; k < j; ++k) s -= st->L[i * CEM_MAX_DIM + k] * st->L[j * CEM_MAX_DIM + k];
-        st->L[i * CEM_MAX_DIM + j] = s / ljj;
+      if (lane == 0) {
+        double d = s_cov[j * CEM_MAX_DIM + j];
+        for (int k = 0; k < j; ++k) d -= s_L[j * CEM_MAX_DIM + k] * s_L[j * CEM_MAX_DIM + k];
+        if (!(d > 0.0)) { s_ok = 0; d = st->min_std[j] * st->min_std[j]; }
+        s_L[j * CEM_MAX_DIM + j] = sqrt(d);
       }
-      for (int i = 0; i < j; ++i) st->L[i * CEM_MAX_DIM + j] = 0.0;
+      __syncwarp();
+      const double ljj = s_L[j * CEM_MAX_DIM + j];
+      for (int i = j + 1 + lane; i < P; i += 32) {
+        double v = s_cov[i * CEM_MAX_DIM + j];
+        for (int k = 0; k < j; ++k) v -= s_L[i * CEM_MAX_DIM + k] * s_L[j * CEM_MAX_DIM + k];
+        s_L[i * CEM_MAX_DIM + j] = v / ljj;
+      }
+      __syncwarp();
     }
-    if (!ok) st->status = 1;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < P * P; q += blockDim.x) {
+    const int i = q / P, j = q % P;
+    st->L[i * CEM_MAX_DIM + j] = j <= i ? s_L[i * CEM_MAX_DIM + j] : 0.0;
+  }
+  if (threadIdx.x == 0) {
+    if (!s_ok) st->status = 1;
     const unsigned b = (unsigned)(keys[0] & 0xFFFFFFFFull);
     const float bc = cost[b];
     if (bc < st->best_cost || (isnan(st->best_cost) && !isnan(bc))) {
