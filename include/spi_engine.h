@@ -57,7 +57,10 @@ extern "C" {
 
 /* Robot model and simulation settings. Leg bodies are ordered FL, FR, RL, RR x hip, thigh,
  * calf (the Isaac Gym DFS order of spigym/config/robot/go2/go2.yaml:29); hip joints rotate
- * about x, thigh and calf joints about y. Inertias are 6 floats xx yy zz xy xz yz. */
+ * about x, thigh and calf joints about y. Inertias are 6 floats xx yy zz xy xz yz.
+ * The kernels take the Go2's joint-origin pattern: hip origins in the base's x-y plane,
+ * thigh origins on the hip's y axis, calf origins on the thigh's z axis, the foot on the
+ * calf's z axis. Every entry point that takes a spi_robot returns SPI_EINVAL for any other. */
 typedef struct spi_robot {
     float body_origin[SPI_N_LEG_BODIES][3]; /* joint origin in the parent frame */
     float body_mass[SPI_N_LEG_BODIES];
