@@ -161,7 +161,7 @@ def _dist():
     return r, r.rank, r.world, r.local
 
 
-def served_vs_plain(specs, realtime, cfg=None, variant="lane3"):
+def served_vs_plain(specs, realtime, cfg=None, variant="lane4"):
     """Run the same jobs served (continuous batching) and plain (one job at a time), both on the
     rollout-kernel variant `variant`."""
     from spi_gb300.workloads import WindowBank, run_plain, run_served
@@ -460,7 +460,7 @@ def run_ours(args):
     if ws == 1 and not args.no_serving:
         from spi_gb300.workloads import c2_specs, small_specs
         from spi_gb300.server import Server
-        sv = variant if variant in Server.VARIANTS else "lane3"
+        sv = variant if variant in Server.VARIANTS else "lane4"
         mix = served_vs_plain(c2_specs(args.mix_jobs, seed=2, iterations=args.mix_iters), False, variant=sv)
         mix["workload"] = (f"{args.mix_jobs} jobs of the c2 size distribution, {args.mix_iters} CEM iterations "
                            "each, all submitted at t=0")

@@ -122,12 +122,12 @@ int spi_set_cost(spi_engine* e, int mode, const float* sq_weights);
  * other. */
 int spi_set_kernel_config(spi_engine* e, int min_blocks);
 
-/* Rollout-kernel lane layout (default after spi_create: SPI_LAYOUT_LANE with min_blocks 3).
+/* Rollout-kernel lane layout (default after spi_create: SPI_LAYOUT_LANE with min_blocks 4).
  * SPI_LAYOUT_QUAD: four lanes per rollout, one leg each, the base
  * solved on all four. SPI_LAYOUT_LANE: one lane per rollout through all four legs, the model
- * in the kernel's parameter block, 66 KB of shared memory per 128-thread CTA (min_blocks 2 or
- * 3; min_blocks 4 keeps the last leg's work record in registers and needs 55 KB). Same equations, results within
- * FP32 rounding of each other; spi_run_trace always uses the quad layout. */
+ * in the kernel's parameter block, 68 KB of shared memory per 128-thread CTA (three CTAs per
+ * SM); min_blocks 2..4 sets the register cap (4: 128 registers). Same equations, results
+ * within FP32 rounding of each other; spi_run_trace always uses the quad layout. */
 #define SPI_LAYOUT_QUAD 0
 #define SPI_LAYOUT_LANE 1
 /* SPI_LAYOUT_BLOCK: the quad layout with each rollout's base solved once per substep by one
@@ -272,11 +272,11 @@ int spi_server_stats(spi_server* s, int32_t* active, size_t* bytes_free);
 int spi_server_set_work_cap(spi_server* s, long long max_items);
 /* Persistent-grid shape: CTAs per SM (0 = occupancy maximum) and work items claimed per atomic. */
 int spi_server_config(spi_server* s, int ctas_per_sm, int items_per_claim);
-/* Rollout-kernel occupancy variant (CTAs of 128 threads per SM: 3 or 4 in the quad layout, 2 or
- * 3 in the lane layout), as spi_set_kernel_config. */
+/* Rollout-kernel occupancy variant (the launch-bounds CTAs per SM: 3 or 4 in the quad layout,
+ * 2 to 4 in the lane layout), as spi_set_kernel_config. */
 int spi_server_set_kernel_config(spi_server* s, int min_blocks);
 /* Rollout-kernel lane layout of the server: SPI_LAYOUT_QUAD (min_blocks 3 or 4) or
- * SPI_LAYOUT_LANE (one lane per rollout, work items of 32 windows; min_blocks 2 or 3), as
+ * SPI_LAYOUT_LANE (one lane per rollout, work items of 32 windows; min_blocks 2 to 4), as
  * spi_set_kernel_layout. Only while no job is held (SPI_ESTATE otherwise). */
 int spi_server_set_kernel_layout(spi_server* s, int layout);
 /* CEM-iteration rounds per tick (1..8, default 1). Each tick runs this many rounds of one

@@ -80,8 +80,11 @@ int spi::run_impl(spi_engine* e, float* trace) {
     else if (e->min_blocks == 3)
       rollout_lane_kernel<3><<<lgrid, 128, kLaneParkBytes, e->stream>>>(e->host_model, win, e->theta.f(), e->N, G,
                                                                         e->partial.f(), bad);
+    else if (motor_shape_of(e->host_model) == kMotorSpeedLimit)
+      rollout_lane_kernel<4, kMotorSpeedLimit><<<lgrid, 128, kLaneParkBytes, e->stream>>>(
+          e->host_model, win, e->theta.f(), e->N, G, e->partial.f(), bad);
     else
-      rollout_lane_kernel<4><<<lgrid, 128, kLanePeelBytes, e->stream>>>(e->host_model, win, e->theta.f(), e->N, G,
+      rollout_lane_kernel<4><<<lgrid, 128, kLaneParkBytes, e->stream>>>(e->host_model, win, e->theta.f(), e->N, G,
                                                                         e->partial.f(), bad);
   } else if (!trace && e->layout == SPI_LAYOUT_BLOCK) {
     if (e->min_blocks == 4)
@@ -138,8 +141,8 @@ int spi_create(const spi_robot* robot, spi_engine** out) {
   rc = e->bad.reserve(sizeof(unsigned long long));
   if (rc) { cudaFree(e->d_model); delete e; return rc; }
   cudaMemset(e->bad.p, 0, sizeof(unsigned long long));
-  // default kernel: the lane layout at 3 CTAs per SM (the fastest on the C1 workload)
-  if ((rc = spi_set_kernel_layout(e, SPI_LAYOUT_LANE)) || (rc = spi_set_kernel_config(e, 3))) {
+  // default kernel: the lane layout at the 128-register cap (the fastest on the C1 workload)
+  if ((rc = spi_set_kernel_layout(e, SPI_LAYOUT_LANE)) || (rc = spi_set_kernel_config(e, 4))) {
     spi_destroy(e);
     return rc;
   }
@@ -232,7 +235,10 @@ int spi_set_kernel_layout(spi_engine* e, int layout) {
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kLaneParkBytes);
     if (ce == cudaSuccess)
       ce = cudaFuncSetAttribute(rollout_lane_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                kLanePeelBytes);
+                                kLaneParkBytes);
+    if (ce == cudaSuccess)
+      ce = cudaFuncSetAttribute(rollout_lane_kernel<4, kMotorSpeedLimit>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, kLaneParkBytes);
     if (ce != cudaSuccess) return cuda_error(ce, "spi_set_kernel_layout: shared-memory attribute");
   } else if (e->min_blocks < 3) {
     e->min_blocks = 3;

@@ -37,62 +37,49 @@ __device__ __forceinline__ float group8_sum(float x) {
 
 // Shared-memory layout per CTA: 16-byte fields, [field][128 threads] throughout, so that each
 // warp access is one conflict-free 128-bit load or store per field:
-//   parking      P legs x kParkVec fields (P = 4, or 3 when the last leg's work record stays in
-//                registers: PEEL, for the 4-CTA-per-SM variant, whose 128-register cap leaves
-//                room for it and whose shared-memory share is 54 KB);
+//   parking      4 legs x kParkVec fields;
 //   leg state a  4 legs x 1 field: (q0, q1, q2, qd0);
 //   targets      4 legs x 1 field: the joint targets of the control step's actions (t0, t1, t2, 0);
-//                with PEEL 3 fields, legs 0..2 in x, y, z and leg 3's three targets in their w;
 //   leg state b  4 legs x one 8-byte field: (qd1, qd2).
-// Offsets below are in 16-byte fields of 128 threads.
-template <bool PEEL> __host__ __device__ constexpr int lane_state_a() { return (PEEL ? 3 : 4) * kParkVec; }
-template <bool PEEL> __host__ __device__ constexpr int lane_act() { return lane_state_a<PEEL>() + 4; }
-template <bool PEEL> __host__ __device__ constexpr int lane_state_b() { return lane_act<PEEL>() + (PEEL ? 3 : 4); }
-template <bool PEEL> __host__ __device__ constexpr int lane_smem_bytes() {
-  return (lane_state_b<PEEL>() + 2) * 128 * (int)sizeof(float4);
-}
-constexpr int kLaneParkBytes = lane_smem_bytes<false>();
-constexpr int kLanePeelBytes = lane_smem_bytes<true>();
+// Offsets below are in 16-byte fields of 128 threads. 136 floats per thread, 68 KB per CTA:
+// three CTAs (12 warps) per SM.
+constexpr int kLaneStateA = 4 * kParkVec;
+constexpr int kLaneTargets = kLaneStateA + 4;
+constexpr int kLaneStateB = kLaneTargets + 4;
+constexpr int kLaneParkBytes = (kLaneStateB + 2) * 128 * (int)sizeof(float4);
 
 // One thread's slots: sm = this thread's first 16-byte field; sb = its first (qd1, qd2) field.
 struct LaneSlots {
   float4* sm;
   float2* sb;
-  template <bool PEEL> __device__ __forceinline__ static LaneSlots of(float4* lane_smem) {
-    return LaneSlots{lane_smem + threadIdx.x,
-                     reinterpret_cast<float2*>(lane_smem + lane_state_b<PEEL>() * 128) + threadIdx.x};
+  __device__ __forceinline__ static LaneSlots of(float4* lane_smem) {
+    return LaneSlots{lane_smem + threadIdx.x, reinterpret_cast<float2*>(lane_smem + kLaneStateB * 128) + threadIdx.x};
   }
-  template <bool PEEL> __device__ __forceinline__ LegState<float> leg_state(int leg) const {
-    const float4 u = sm[(lane_state_a<PEEL>() + leg) * 128];
+  __device__ __forceinline__ LegState<float> leg_state(int leg) const {
+    const float4 u = sm[(kLaneStateA + leg) * 128];
     const float2 v = sb[leg * 128];
     LegState<float> L;
     L.q[0] = u.x; L.q[1] = u.y; L.q[2] = u.z;
     L.qd[0] = u.w; L.qd[1] = v.x; L.qd[2] = v.y;
     return L;
   }
-  template <bool PEEL> __device__ __forceinline__ void put_leg_state(int leg, const LegState<float>& L) const {
-    sm[(lane_state_a<PEEL>() + leg) * 128] = make_float4(L.q[0], L.q[1], L.q[2], L.qd[0]);
+  __device__ __forceinline__ void put_leg_state(int leg, const LegState<float>& L) const {
+    sm[(kLaneStateA + leg) * 128] = make_float4(L.q[0], L.q[1], L.q[2], L.qd[0]);
     sb[leg * 128] = make_float2(L.qd[1], L.qd[2]);
   }
   __device__ __forceinline__ float4* park(int leg) const { return sm + leg * kParkVec * 128; }
   // the joint targets of the twelve actions of one control step (legs in order)
-  template <bool PEEL> __device__ __forceinline__ void put_targets(const DevModel& M, const float4 a0,
-                                                                    const float4 a1, const float4 a2) const {
+  __device__ __forceinline__ void put_targets(const DevModel& M, const float4 a0, const float4 a1,
+                                              const float4 a2) const {
     const float a[12] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w, a2.x, a2.y, a2.z, a2.w};
     float t[12];
 #pragma unroll
     for (int j = 0; j < 12; ++j) t[j] = joint_target(M, j % 3, j / 3, a[j]);
-    float4* p = sm + lane_act<PEEL>() * 128;
-    if (PEEL) {
-      p[0] = make_float4(t[0], t[1], t[2], t[9]);
-      p[128] = make_float4(t[3], t[4], t[5], t[10]);
-      p[256] = make_float4(t[6], t[7], t[8], t[11]);
-    } else {
-      p[0] = make_float4(t[0], t[1], t[2], 0.f);
-      p[128] = make_float4(t[3], t[4], t[5], 0.f);
-      p[256] = make_float4(t[6], t[7], t[8], 0.f);
-      p[384] = make_float4(t[9], t[10], t[11], 0.f);
-    }
+    float4* p = sm + kLaneTargets * 128;
+    p[0] = make_float4(t[0], t[1], t[2], 0.f);
+    p[128] = make_float4(t[3], t[4], t[5], 0.f);
+    p[256] = make_float4(t[6], t[7], t[8], 0.f);
+    p[384] = make_float4(t[9], t[10], t[11], 0.f);
   }
 };
 
@@ -112,49 +99,38 @@ __device__ __forceinline__ void store_gains(const LegGains<float>& r, float4* g)
 
 // One physics substep of one rollout on one lane. s: this thread's slots; bp: the warp's base
 // parameters; gains: the warp's four legs' LegGains (two fields each).
-template <bool PEEL, int MS>
+template <int MS>
 __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>& B, const LaneSlots& s,
                                              const BaseParams<float>* bp, const float4* gains) {
-  constexpr int NP = PEEL ? 3 : 4;
   // articulated inertia and bias force at the base: the base body's own, plus each leg's
   LegOut<float> sum = base_terms(*bp, B);
-  const float4* tgt = s.sm + lane_act<PEEL>() * 128;
+  const float4* tgt = s.sm + kLaneTargets * 128;
   const bool corners = corners_may_touch(M, B);
 #pragma unroll 1
-  for (int leg = 0; leg < NP; ++leg) {
+  for (int leg = 0; leg < 4; ++leg) {
     const LegGains<float> P = load_gains(gains + 2 * leg);
     const float4 a = tgt[leg * 128];
     const float a3[3] = {a.x, a.y, a.z};
     ParkedWork pw{s.park(leg), 128};
-    phase_a_into<MS>(M, leg, B, s.leg_state<PEEL>(leg), P, a3, pw, sum, corners);
-  }
-  LegWork<float> w3;
-  if (PEEL) {
-    const float a3[3] = {tgt[0].w, tgt[128].w, tgt[256].w};
-    phase_a_into<MS>(M, 3, B, s.leg_state<PEEL>(3), load_gains(gains + 6), a3, w3, sum, corners);
+    phase_a_into<MS>(M, leg, B, s.leg_state(leg), P, a3, pw, sum, corners);
   }
   const SV<float> a0 = base_solve(M, sum.I, sum.p, B);
-  if (PEEL) {
-    LegState<float> L = s.leg_state<PEEL>(3);
-    phase_c(M, 3, a0, w3, L);
-    s.put_leg_state<PEEL>(3, L);
-  }
 #pragma unroll 1
-  for (int leg = 0; leg < NP; ++leg) {
-    LegState<float> L = s.leg_state<PEEL>(leg);
+  for (int leg = 0; leg < 4; ++leg) {
+    LegState<float> L = s.leg_state(leg);
     LegWork<float> lw;
     unpark_legwork(lw, s.park(leg), 128);
     phase_c(M, leg, a0, lw, L);
-    s.put_leg_state<PEEL>(leg, L);
+    s.put_leg_state(leg, L);
   }
 }
 
 // One warp: theta th13 against windows [32 wb, 32 wb + 32) of win, writing the partials of the
 // four eight-window groups g = 4 wb .. 4 wb + 3 (those below G) to partial_n[g][SPI_N_COMP].
-// lane_smem: the CTA's lane_smem_bytes<PEEL>() of dynamic shared memory; bp_warp / gains_warp: the
+// lane_smem: the CTA's kLaneParkBytes of dynamic shared memory; bp_warp / gains_warp: the
 // CTA's per-warp parameter slots. MS: the motor shape (motor_shape_of the model, or
 // kMotorRuntime). Callable repeatedly by one warp (persistent kernels).
-template <bool PEEL, int MS = kMotorRuntime>
+template <int MS = kMotorRuntime>
 __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinView& win, const float* th13, int wb,
                                                   float* partial_n, int G, unsigned long long* n_bad,
                                                   float4* lane_smem, BaseParams<float>* bp_warp,
@@ -175,7 +151,7 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
     __syncwarp();
   }
 
-  const LaneSlots sl = LaneSlots::of<PEEL>(lane_smem);
+  const LaneSlots sl = LaneSlots::of(lane_smem);
   BaseState<float> B;
   {
     float s13[13];
@@ -190,18 +166,18 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
         L.q[k] = __ldg(win.init + (13 + 3 * leg + k) * W + w);
         L.qd[k] = __ldg(win.init + (25 + 3 * leg + k) * W + w);
       }
-      sl.put_leg_state<PEEL>(leg, L);
+      sl.put_leg_state(leg, L);
     }
   }
   const int dec = M.decimation;
   for (int h = 0; h < H; ++h) {
     const float4* ap = reinterpret_cast<const float4*>(win.act + ((size_t)h * W + w) * 12);
-    sl.put_targets<PEEL>(M, __ldg(ap), __ldg(ap + 1), __ldg(ap + 2));
-    for (int s = 0; s < dec; ++s) substep_lane<PEEL, MS>(M, B, sl, &bp_warp[wib], gains_warp[wib]);
+    sl.put_targets(M, __ldg(ap), __ldg(ap + 1), __ldg(ap + 2));
+    for (int s = 0; s < dec; ++s) substep_lane<MS>(M, B, sl, &bp_warp[wib], gains_warp[wib]);
   }
   LegState<float> L[4];
 #pragma unroll
-  for (int leg = 0; leg < 4; ++leg) L[leg] = sl.leg_state<PEEL>(leg);
+  for (int leg = 0; leg < 4; ++leg) L[leg] = sl.leg_state(leg);
   // final-step error components of this lane's window
   float s13[13];
   base_to_world(B, s13);
@@ -237,20 +213,22 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
 
 // One warp per (theta n, block of 32 windows); grid covers N * ceil(W / 32) warps; G is the
 // number of eight-window groups (ceil(W / 8)) of the partial layout. CTAs of 128 threads with
-// lane_smem_bytes<(MINB >= 4)>() of dynamic shared memory.
+// kLaneParkBytes of dynamic shared memory. MINB sets the register cap (2: ~200, 3: 168, 4: 128);
+// shared memory holds every variant to three CTAs per SM, and at 128 registers the code still
+// needs no spills.
 template <int MINB, int MS = kMotorRuntime>
 __global__ void __launch_bounds__(128, MINB) rollout_lane_kernel(const __grid_constant__ DevModel M, WinView win,
                                                                  const float* __restrict__ theta, int N, int G,
                                                                  float* __restrict__ partial,
                                                                  unsigned long long* __restrict__ n_bad) {
-  extern __shared__ float4 lane_smem[];              // lane_smem_bytes<(MINB >= 4)>()
+  extern __shared__ float4 lane_smem[];              // kLaneParkBytes
   __shared__ BaseParams<float> bp_warp[4];
   __shared__ float4 gains_warp[4][8];
   const int WB = (win.W + 31) >> 5;
   const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (warp >= (long long)N * WB) return;   // uniform per warp
   const int n = (int)(warp / WB), wb = (int)(warp % WB);
-  rollout_lane_warp<(MINB >= 4), MS>(M, win, theta + (size_t)n * SPI_THETA_DIM, wb, partial + (size_t)n * G * SPI_N_COMP,
+  rollout_lane_warp<MS>(M, win, theta + (size_t)n * SPI_THETA_DIM, wb, partial + (size_t)n * G * SPI_N_COMP,
                                  G, n_bad, lane_smem, bp_warp, gains_warp);
 }
 

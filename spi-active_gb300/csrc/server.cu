@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(128, MINB) server_rollout_lane_kernel(const __
       const long long local = item - begin[order[lo]];
       const int WB = (S.win.W + 31) >> 5;
       const int n = (int)(local / WB), wb = (int)(local % WB);
-      rollout_lane_warp<false, MS>(M, S.win, S.theta + (size_t)n * SPI_THETA_DIM, wb,
+      rollout_lane_warp<MS>(M, S.win, S.theta + (size_t)n * SPI_THETA_DIM, wb,
                                S.partial + (size_t)n * S.G * SPI_N_COMP, S.G, n_bad, lane_smem, bp_warp, gains_warp);
     }
   }
@@ -280,14 +280,21 @@ int enqueue_tick(spi_server* s) {
   for (int r = 0; r < s->rounds; ++r) {
     cem_sample_kernel<<<dim3(rows, s->max_slots), 128, 0, s->stream>>>(s->d_cem, s->d_rounds, r);
     if (s->layout == SPI_LAYOUT_LANE) {
+      const bool sl = motor_shape_of(s->host_model) == kMotorSpeedLimit;
       if (s->min_blocks <= 2)
         server_rollout_lane_kernel<2><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
             s->host_model, s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
-      else if (motor_shape_of(s->host_model) == kMotorSpeedLimit)
+      else if (s->min_blocks == 3 && sl)
         server_rollout_lane_kernel<3, kMotorSpeedLimit><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
             s->host_model, s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
-      else
+      else if (s->min_blocks == 3)
         server_rollout_lane_kernel<3><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
+            s->host_model, s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
+      else if (sl)
+        server_rollout_lane_kernel<4, kMotorSpeedLimit><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
+            s->host_model, s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
+      else
+        server_rollout_lane_kernel<4><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
             s->host_model, s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
     } else if (s->min_blocks == 4) {
       server_rollout_kernel<4><<<s->grid, 128, 0, s->stream>>>(s->d_model, s->d_slots, s->d_order, s->d_begin,
@@ -328,9 +335,12 @@ int resize_grid(spi_server* s) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaError_t ce;
   if (s->layout == SPI_LAYOUT_LANE)
-    ce = s->min_blocks <= 2
-             ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_lane_kernel<2>, 128, kLaneParkBytes)
-             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_lane_kernel<3>, 128, kLaneParkBytes);
+    ce = s->min_blocks <= 2   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_lane_kernel<2>, 128,
+                                                                                kLaneParkBytes)
+         : s->min_blocks == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_lane_kernel<3>, 128,
+                                                                                kLaneParkBytes)
+                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_lane_kernel<4>, 128,
+                                                                                kLaneParkBytes);
   else
     ce = s->min_blocks == 4 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_kernel<4>, 128, 0)
                             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_kernel<3>, 128, 0);
@@ -443,7 +453,7 @@ int spi_server_config(spi_server* s, int ctas_per_sm, int items_per_claim) {
 
 int spi_server_set_kernel_config(spi_server* s, int min_blocks) {
   if (!s) return set_error(SPI_EINVAL, "null server");
-  const int lo = s->layout == SPI_LAYOUT_LANE ? 2 : 3, hi = s->layout == SPI_LAYOUT_LANE ? 3 : 4;
+  const int lo = s->layout == SPI_LAYOUT_LANE ? 2 : 3, hi = 4;
   if (min_blocks < lo || min_blocks > hi)
     return set_error(SPI_EINVAL, "spi_server_set_kernel_config: min_blocks %d outside [%d, %d]", min_blocks, lo, hi);
   s->min_blocks = min_blocks;
@@ -474,8 +484,14 @@ int spi_server_set_kernel_layout(spi_server* s, int layout) {
     if (ce == cudaSuccess)
       ce = cudaFuncSetAttribute(server_rollout_lane_kernel<3, kMotorSpeedLimit>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize, kLaneParkBytes);
+    if (ce == cudaSuccess)
+      ce = cudaFuncSetAttribute(server_rollout_lane_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                kLaneParkBytes);
+    if (ce == cudaSuccess)
+      ce = cudaFuncSetAttribute(server_rollout_lane_kernel<4, kMotorSpeedLimit>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, kLaneParkBytes);
     if (ce != cudaSuccess) return cuda_error(ce, "spi_server_set_kernel_layout: shared-memory attribute");
-    s->min_blocks = std::min(std::max(s->min_blocks, 2), 3);
+    s->min_blocks = std::min(std::max(s->min_blocks, 2), 4);
   } else {
     s->min_blocks = std::min(std::max(s->min_blocks, 3), 4);
   }

@@ -158,7 +158,7 @@ class Server:
         _lib.check(self.lib.spi_server_set_rounds(self._h, int(rounds)))
 
     # rollout-kernel variants the server runs, by the autotuner's names
-    VARIANTS = {"quad3": (0, 3), "quad4": (0, 4), "lane2": (1, 2), "lane3": (1, 3)}
+    VARIANTS = {"quad3": (0, 3), "quad4": (0, 4), "lane2": (1, 2), "lane3": (1, 3), "lane4": (1, 4)}
 
     def set_variant(self, name):
         layout, min_blocks = self.VARIANTS[name]

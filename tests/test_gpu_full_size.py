@@ -79,7 +79,7 @@ def test_lane_and_quad_layouts_agree_at_full_size(c1):
     try:
         other = e.evaluate(th)[1].cpu().numpy()
     finally:
-        set_variant(e, "lane3")
+        set_variant(e, "lane4")
     assert _rel(other, cost.cpu().numpy()) <= 1e-5
 
 

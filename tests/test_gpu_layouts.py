@@ -62,7 +62,7 @@ def test_layout_matches_oracle_h20(built, variant):
     assert cost_error(cost.cpu().numpy(), oc.scalar_cost(refc)) <= 1e-4
 
 
-@pytest.mark.parametrize("variant", ("lane3", "block4"))
+@pytest.mark.parametrize("variant", ("lane4", "block4"))
 @pytest.mark.parametrize("W,H,N", [(1, 1, 1), (13, 3, 5), (33, 2, 9), (64, 5, 3)])
 def test_layout_ragged_sizes(built, W, H, N, variant):
     rng = np.random.default_rng(W * 10 + H)
@@ -77,10 +77,11 @@ def test_layout_ragged_sizes(built, W, H, N, variant):
 @pytest.mark.parametrize("kw", [dict(tanh_a=(15.0, 18.0, 25.0), hip_action_scale=0.5),
                                 dict(motor_gain=(0.9, 1.1, 1.05), torque_speed=False),
                                 dict(torque_speed=False)])
-def test_lane3_motor_models_match_oracle(built, kw):
-    """lane3 runs a kernel specialised to the default motor model (torque-speed limit, unit
-    gains, no tanh saturation) and the run-time-flag kernel for any other; each motor model
-    here takes the latter, against the FP64 oracle with the same settings, over H = 10."""
+def test_lane_motor_models_match_oracle(built, kw):
+    """The lane kernels run an instantiation specialised to the default motor model (torque-speed
+    limit, unit gains, no tanh saturation) and the run-time-flag kernel for any other; each
+    motor model here takes the latter, against the FP64 oracle with the same settings, over
+    H = 10."""
     from spi_gb300.autotune import set_variant
     from spi_gb300.engine import Engine
     from spi_gb300.robot import SimConfig
@@ -91,7 +92,7 @@ def test_lane3_motor_models_match_oracle(built, kw):
     th = random_theta(rng, 16).astype(np.float32)
     e = Engine(SimConfig(**kw))
     e.load_windows(torch.from_numpy(init), torch.from_numpy(actions), torch.from_numpy(target))
-    set_variant(e, "lane3")
+    set_variant(e, "lane4")
     comp, cost = e.evaluate(torch.from_numpy(th))
     assert e.sync() == 0
     N, W = th.shape[0], init.shape[0]
@@ -116,7 +117,7 @@ def test_layouts_agree(built):
         assert cost_error(costs[v], costs["quad3"]) <= 1e-5, v
 
 
-@pytest.mark.parametrize("variant", ("lane3", "block4"))
+@pytest.mark.parametrize("variant", ("lane4", "block4"))
 def test_layout_reference_cost_mode_and_mask(built, variant):
     from oracle import windows as ow
     from spi_gb300.engine import COST_REF
@@ -132,7 +133,7 @@ def test_layout_reference_cost_mode_and_mask(built, variant):
     assert cost_error(cost.cpu().numpy(), oc.compute_cost(refm[:, :3])) <= 1e-4
 
 
-@pytest.mark.parametrize("variant", ("lane3", "block4"))
+@pytest.mark.parametrize("variant", ("lane4", "block4"))
 def test_layout_deterministic_and_counts_nonfinite(built, variant):
     rng = np.random.default_rng(8)
     _, init, actions, target = oracle_windows(3, n_traj=2, T=40, H=10)
@@ -155,7 +156,7 @@ def test_layouts_under_cem_graph(built):
     from spi_gb300.engine import Engine
     _, init, actions, target = oracle_windows(4, n_traj=2, T=30, H=8)
     res = {}
-    for v in ("quad3", "lane3", "block4"):
+    for v in ("quad3", "lane4", "block4"):
         e = Engine()
         e.load_windows(torch.from_numpy(init), torch.from_numpy(actions), torch.from_numpy(target))
         set_variant(e, v)
@@ -164,6 +165,6 @@ def test_layouts_under_cem_graph(built):
         cem.run(3, graph=True)
         res[v] = cem.read()
     # the first iteration's population is identical; later ones may part at the ulp level
-    for v in ("lane3", "block4"):
+    for v in ("lane4", "block4"):
         assert np.isfinite(res[v]["best_cost"])
         assert abs(np.log(res[v]["best_cost"] / res["quad3"]["best_cost"])) < np.log(10.0)

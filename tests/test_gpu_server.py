@@ -31,7 +31,7 @@ def _server(variant="quad3", **kw):
     return s
 
 
-@pytest.mark.parametrize("variant", ["quad3", "lane3"])
+@pytest.mark.parametrize("variant", ["quad3", "lane4"])
 def test_same_result_alone_and_in_the_mix(built, variant):
     specs = [(1, 24, 5, 64, [0], 11), (2, 40, 9, 128, [0, 4, 5, 6], 12), (3, 16, 3, 96, list(range(13)), 13)]
     mix = _run(_server(variant, max_slots=8, max_samples=256), [_job(*s, iters=4) for s in specs])
@@ -43,7 +43,7 @@ def test_same_result_alone_and_in_the_mix(built, variant):
         assert np.array_equal(r["mu"], alone["mu"])
 
 
-@pytest.mark.parametrize("variant", ["quad3", "lane3"])
+@pytest.mark.parametrize("variant", ["quad3", "lane4"])
 def test_server_job_equals_engine_cem(built, variant):
     """A server job and the single-job engine CEM agree within the 1e-4 relative cost bar.
 
@@ -95,7 +95,7 @@ def test_admission_respects_budget_and_slots(built):
     assert small.submit(job) is None                  # over the HBM budget
 
 
-@pytest.mark.parametrize("variant", ["quad3", "lane3"])
+@pytest.mark.parametrize("variant", ["quad3", "lane4"])
 def test_rounds_per_tick_do_not_change_results(built, variant):
     """Jobs advanced several CEM iterations per tick reach bitwise the same results."""
     specs = [(9, 64, 12, 256, [0, 4], 51), (10, 8, 3, 64, [0], 52), (11, 16, 5, 64, [0, 1, 2], 53)]
@@ -113,7 +113,7 @@ def test_rounds_per_tick_do_not_change_results(built, variant):
 
 def test_small_job_takes_several_iterations_per_tick(built):
     """Beside a job with 64x its work per iteration, a small job takes 4 iterations per tick."""
-    s = _server("lane3", max_slots=4, max_samples=512)
+    s = _server("lane4", max_slots=4, max_samples=512)
     s.set_rounds(4)
     big, keep_big = _job(12, 128, 16, 512, [0, 4], 61, iters=12)
     small, keep_small = _job(13, 8, 2, 64, [0], 62, iters=12)
