@@ -248,11 +248,6 @@ template <class T> SPI_INL void add_to(Art<T>& a, const Art<T>& b) {
 // Rigid-body inertia as mass, first moment h = m c and rotational inertia about the body
 // origin (10 numbers; sums of rigid bodies stay rigid, so composite inertias use it too).
 template <class T> struct RI { T m; V3<T> h; S3<T> I; };
-template <class T> SPI_INL void ri_add(RI<T>& a, const RI<T>& b) {
-  a.m = a.m + b.m;
-  a.h = a.h + b.h;
-  a.I.xx += b.I.xx; a.I.yy += b.I.yy; a.I.zz += b.I.zz; a.I.xy += b.I.xy; a.I.xz += b.I.xz; a.I.yz += b.I.yz;
-}
 template <class T> SPI_INL SV<T> ri_mul(const RI<T>& a, const SV<T>& v) { return rigid_mul(a.m, a.h, a.I, v); }
 template <class T> SPI_INL SV<T> ri_mul_acc(const RI<T>& a, const SV<T>& v, const SV<T>& acc) {
   return rigid_mul_acc(a.m, a.h, a.I, v, acc);
@@ -271,13 +266,6 @@ template <class T> SPI_INL Art<T> ri_art(const RI<T>& a) { return rigid(a.m, a.h
 // (calf joints), RM = 3: in the x-y plane (hip joints), RM = 7: general. The model builder
 // checks the pattern.
 constexpr int kHipRM = 3;
-// r x u for an origin r with zero components skipped.
-template <int RM, class T> SPI_INL V3<T> rcross(V3<T> r, V3<T> u) {
-  if (RM == 2) return v3(r.y * u.z, T(0), -(r.y * u.x));
-  if (RM == 4) return v3(-(r.z * u.y), r.z * u.x, T(0));
-  if (RM == 3) return v3(r.y * u.z, -(r.x * u.z), r.x * u.y - r.y * u.x);
-  return cross(r, u);
-}
 // u - r x w, with the known-zero terms of r x w not subtracted.
 template <int RM, class T> SPI_INL V3<T> sub_rcross(V3<T> u, V3<T> r, V3<T> w) {
   if (RM == 2) return v3(u.x - r.y * w.z, u.y, u.z + r.y * w.x);
@@ -321,14 +309,6 @@ template <int AX, int RM = 7, class T> SPI_INL SV<T> motion_to_child(const SV<T>
   SV<T> o;
   o.w = rotT<AX>(c, s, m.w);
   o.v = rotT<AX>(c, s, sub_rcross<RM>(m.v, r, m.w));
-  return o;
-}
-// acc + X m.
-template <int AX, int RM = 7, class T>
-SPI_INL SV<T> motion_to_child_acc(const SV<T>& m, T c, T s, V3<T> r, const SV<T>& acc) {
-  SV<T> o;
-  o.w = rotT_acc<AX>(c, s, m.w, acc.w);
-  o.v = rotT_acc<AX>(c, s, sub_rcross<RM>(m.v, r, m.w), acc.v);
   return o;
 }
 
@@ -678,14 +658,6 @@ template <class T> SPI_INL T motor_torque(const DevModel& M, const LegParams<T>&
 
 template <class T> SPI_INL V3<T> leg_org(const DevModel& M, int k, int leg) {
   return v3(T(M.org[k][0][leg]), T(M.org[k][1][leg]), T(M.org[k][2][leg]));
-}
-template <class T> SPI_INL RI<T> leg_ri(const DevModel& M, int k, int leg) {
-  RI<T> r;
-  r.m = T(M.m[k][leg]);
-  r.h = v3(T(M.h[k][0][leg]), T(M.h[k][1][leg]), T(M.h[k][2][leg]));
-  r.I.xx = T(M.I[k][0][leg]); r.I.yy = T(M.I[k][1][leg]); r.I.zz = T(M.I[k][2][leg]);
-  r.I.xy = T(M.I[k][3][leg]); r.I.xz = T(M.I[k][4][leg]); r.I.yz = T(M.I[k][5][leg]);
-  return r;
 }
 
 // The same constants from a leg's packed slots (DevModel::legc).
