@@ -8,7 +8,6 @@
 // lanes and no shuffles combine the legs; the model is passed by value in the kernel's
 // parameter block.
 //
-//
 // The error components of each window are formed at the final step, summed over each group
 // of eight lanes with xor-shuffles (the same tree as the quad layout's slot sum) and written
 // as one partial per (theta, window group): the partial layout, and so finalize_costs, is
@@ -31,9 +30,10 @@ __device__ __forceinline__ float group8_sum(float x) {
 
 // Code size and register budget: the four legs run in a loop that is not unrolled (four
 // unrolled copies of phase A overflow the instruction cache), so per-leg data is indexed at run
-// time: each leg's joint state, work record and actions live in shared memory, and the
-// model's per-leg constants are indexed loads from the kernel's parameter block. The
-// theta-derived base and leg parameters are one copy per warp (all lanes share theta).
+// time: each leg's joint state, work record and joint targets live in shared memory, and the
+// model's per-leg constants are 16-byte loads from the kernel's parameter block (DevModel::legc).
+// The theta-derived base parameters and leg gains are one copy per warp (all lanes share
+// theta).
 
 // Shared-memory layout per CTA: 16-byte fields, [field][128 threads] throughout, so that each
 // warp access is one conflict-free 128-bit load or store per field:
