@@ -117,7 +117,11 @@ static __global__ void __launch_bounds__(1024) cem_refit_kernel(CemState* __rest
   for (int i = threadIdx.x; i < npad; i += blockDim.x)
     keys[i] = i < N ? cost_key(cost[i], (unsigned)i) : ~0ull;
   __syncthreads();
-  // bitonic sort, ascending
+  // bitonic sort, ascending. Thread t handles keys t, t + blockDim.x, ...; for a partner
+  // distance j < 32 both keys of a pair lie in one 32-key block that one warp handles, so a stage
+  // followed by such a stage orders with a warp barrier. A stage followed by one of distance
+  // >= 32 (every j >= 32, and the last stage j = 1 of a round k >= 32, whose successor has
+  // j = 2k / 2 >= 32) takes the CTA barrier.
   for (int k = 2; k <= npad; k <<= 1) {
     for (int j = k >> 1; j > 0; j >>= 1) {
       for (int i = threadIdx.x; i < npad; i += blockDim.x) {
@@ -128,9 +132,10 @@ static __global__ void __launch_bounds__(1024) cem_refit_kernel(CemState* __rest
           if ((a > b) == up) { keys[i] = b; keys[l] = a; }
         }
       }
-      __syncthreads();
+      if (j >= 32 || (j == 1 && k >= 32)) __syncthreads(); else __syncwarp();
     }
   }
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
   // elite mean, one warp per dimension
   for (int d = warp; d < P; d += nwarps) {
