@@ -86,12 +86,12 @@ template <class T> SPI_INL T m_div_c(T x, float d, float dinv) { (void)dinv; ret
 // (a b) x; every other scalar type forms a b in its own precision.
 SPI_INL float m_mul2_c(float x, float a, float b, float ab) { (void)a; (void)b; return ab * x; }
 template <class T> SPI_INL T m_mul2_c(T x, float a, float b, float ab) { (void)ab; return T(a) * T(b) * x; }
-// Device FP32: reduce to [-pi, pi] (joint angles stay within a few radians), then the MUFU
-// sine / cosine, whose absolute error there is ~2^-21.
+// Device FP32: the MUFU sine / cosine. Joint angles stay within a few radians (the PD targets
+// lie within action_clip * action_scale of the default pose), where their absolute error is
+// ~2^-21 for |x| <= pi and ~2^-20.5 out to many periods, so no range reduction is applied.
 SPI_INL void m_sincos(float x, float* s, float* c) {
 #if defined(__CUDA_ARCH__)
-  const float r = fmaf(-6.28318530717958648f, rintf(x * 0.159154943091895336f), x);
-  __sincosf(r, s, c);
+  __sincosf(x, s, c);
 #else
   *s = sinf(x); *c = cosf(x);
 #endif
