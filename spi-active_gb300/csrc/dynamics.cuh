@@ -581,7 +581,8 @@ template <class T> SPI_INL LegParams<T> leg_params(const T* th, int leg) {
 template <class T> SPI_INL V3<T> contact_force(const DevModel& M, T radius, T z, V3<T> v, T* mimp) {
   T pen = radius - z;
   T s = m_clamp(pen * T(M.ramp_inv), T(0), T(1));
-  T fn = m_sel(pen > T(0), m_fmax(T(0), T(M.k) * pen - T(M.c) * s * v.z), T(0));
+  // (for pen <= 0 the ramp s is 0 and k pen <= 0, so the max is 0: no contact, no select)
+  T fn = m_fmax(T(0), T(M.k) * pen - T(M.c) * s * v.z);
   T vtn = m_sqrt(v.x * v.x + v.y * v.y);
   T lim = T(M.mu) * fn;
   T scale = m_sel(T(M.ct) * vtn <= lim, T(M.ct), lim / vtn);
@@ -598,7 +599,7 @@ template <class T> SPI_INL V3<T> contact_force_local(const DevModel& M, T radius
   const V3<T> vt = v3(v.x - vz * n.x, v.y - vz * n.y, v.z - vz * n.z);
   T pen = radius - z;
   T s = m_clamp(pen * T(M.ramp_inv), T(0), T(1));
-  T fn = m_sel(pen > T(0), m_fmax(T(0), T(M.k) * pen - T(M.c) * s * vz), T(0));
+  T fn = m_fmax(T(0), T(M.k) * pen - T(M.c) * s * vz);
   T vtn = m_sqrt(dot(vt, vt));
   T lim = T(M.mu) * fn;
   T scale = m_sel(T(M.ct) * vtn <= lim, T(M.ct), lim / vtn);
