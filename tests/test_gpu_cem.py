@@ -22,9 +22,10 @@ def _setup(P=13, N=256, seed=11, alpha=1.0, H=5, theta_true=None):
     return e, cem, ids
 
 
-@pytest.mark.parametrize("P", [1, 5, 13])
-def test_sampling_and_refit_match_oracle(built, P):
-    N, seed = 256, 11
+@pytest.mark.parametrize("P,N", [(1, 256), (5, 256), (13, 256), (13, 3000), (13, 4096)])
+def test_sampling_and_refit_match_oracle(built, P, N):
+    """N = 3000 pads the sort to 4096 keys; 3000 and 4096 put four keys on each sort thread."""
+    seed = 11
     e, cem, ids = _setup(P=P, N=N, seed=seed, alpha=0.9)
     lo, hi = gm.THETA_PRIOR_LO[ids], gm.THETA_PRIOR_HI[ids]
     # iteration 0: uniform prior box
