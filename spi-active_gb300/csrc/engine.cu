@@ -69,7 +69,7 @@ int spi::run_impl(spi_engine* e, float* trace) {
   const unsigned grid = blocks_for(warps, 4);
   unsigned long long* bad = (unsigned long long*)e->bad.p;
   if (!trace && e->layout == SPI_LAYOUT_LANE) {
-    const long long lwarps = (long long)e->N * ((e->W + 31) / 32);
+    const long long lwarps = ((long long)e->N * G + 3) / 4;   // four (theta, 8-window group) items a warp
     const unsigned lgrid = blocks_for(lwarps, 4);
     if (e->min_blocks <= 2)
       rollout_lane_kernel<2><<<lgrid, 128, kLaneParkBytes, e->stream>>>(e->host_model, win, e->theta.f(), e->N, G,

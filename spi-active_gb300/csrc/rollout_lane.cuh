@@ -125,29 +125,37 @@ __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>
   }
 }
 
-// One warp: theta th13 against windows [32 wb, 32 wb + 32) of win, writing the partials of the
-// four eight-window groups g = 4 wb .. 4 wb + 3 (those below G) to partial_n[g][SPI_N_COMP].
-// lane_smem: the CTA's kLaneParkBytes of dynamic shared memory; bp_warp / gains_warp: the
-// CTA's per-warp parameter slots. MS: the motor shape (motor_shape_of the model, or
-// kMotorRuntime). Callable repeatedly by one warp (persistent kernels).
+// One warp: four consecutive items of the flattened list of (theta n, eight-window group g)
+// pairs, n * G + g for g < G = ceil(W / 8), starting at item g0; eight lanes per item, one
+// window each. Items may belong to different theta samples, so a window set with few windows
+// still fills the warp. Writes each item's weighted error components to
+// partial[(n G + g)][SPI_N_COMP]. theta: [N][SPI_THETA_DIM]. lane_smem: the CTA's
+// kLaneParkBytes of dynamic shared memory; bp_warp / gains_warp: the CTA's per-warp, per-item
+// parameter slots. MS: the motor shape (motor_shape_of the model, or kMotorRuntime).
+// Callable repeatedly by one warp (persistent kernels).
 template <int MS = kMotorRuntime>
-__device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinView& win, const float* th13, int wb,
-                                                  float* partial_n, int G, unsigned long long* n_bad,
-                                                  float4* lane_smem, BaseParams<float>* bp_warp,
-                                                  float4 (*gains_warp)[8]) {
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+__device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinView& win, const float* theta,
+                                                  long long g0, int N, float* partial, int G,
+                                                  unsigned long long* n_bad, float4* lane_smem,
+                                                  BaseParams<float> (*bp_warp)[4], float4 (*gains_warp)[4][8]) {
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, grp = lane >> 3, sub = lane & 7;
   const int W = win.W, H = win.H;
-  int w = wb * 32 + lane;
-  const bool active = w < W;
-  if (!active) w = W - 1;
+  const long long items = (long long)N * G;
+  long long q = g0 + grp;
+  const bool item_live = q < items;
+  if (!item_live) q = items - 1;
+  const int n = (int)(q / G), g = (int)(q % G);
+  int w = g * 8 + sub;
+  const bool active = item_live && w < W;
+  if (w >= W) w = W - 1;
 
   __syncwarp();                      // the warp's previous item has finished with its slots
   {
     float th[SPI_THETA_DIM];
 #pragma unroll
-    for (int i = 0; i < SPI_THETA_DIM; ++i) th[i] = __ldg(th13 + i);
-    if (lane == 0) bp_warp[wib] = base_params<float>(M, th);
-    if (lane < 4) store_gains(leg_gains(M, leg_params<float>(th, lane), lane), gains_warp[wib] + 2 * lane);
+    for (int i = 0; i < SPI_THETA_DIM; ++i) th[i] = __ldg(theta + (size_t)n * SPI_THETA_DIM + i);
+    if (sub == 0) bp_warp[wib][grp] = base_params<float>(M, th);
+    if (sub < 4) store_gains(leg_gains(M, leg_params<float>(th, sub), sub), gains_warp[wib][grp] + 2 * sub);
     __syncwarp();
   }
 
@@ -173,7 +181,7 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
   for (int h = 0; h < H; ++h) {
     const float4* ap = reinterpret_cast<const float4*>(win.act + ((size_t)h * W + w) * 12);
     sl.put_targets(M, __ldg(ap), __ldg(ap + 1), __ldg(ap + 2));
-    for (int s = 0; s < dec; ++s) substep_lane<MS>(M, B, sl, &bp_warp[wib], gains_warp[wib]);
+    for (int s = 0; s < dec; ++s) substep_lane<MS>(M, B, sl, &bp_warp[wib][grp], gains_warp[wib][grp]);
   }
   LegState<float> L[4];
 #pragma unroll
@@ -202,17 +210,16 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
   if (active && !finite) atomicAdd(n_bad, 1ull);
   const float wt = active ? __ldg(win.weight + w) : 0.f;
   const float comp[SPI_N_COMP] = {sqrtf(sp), sqrtf(sq), sqrtf(sj), sp, sq, sv, sw, sj, sjd};
-  const int g = wb * 4 + (lane >> 3);
-  float* out = partial_n + (size_t)g * SPI_N_COMP;
+  float* out = partial + ((size_t)n * G + g) * SPI_N_COMP;
 #pragma unroll
   for (int k = 0; k < SPI_N_COMP; ++k) {
     const float v = group8_sum(active ? comp[k] * wt : 0.f);
-    if ((lane & 7) == 0 && g < G) out[k] = v;
+    if (sub == 0 && item_live) out[k] = v;
   }
 }
 
-// One warp per (theta n, block of 32 windows); grid covers N * ceil(W / 32) warps; G is the
-// number of eight-window groups (ceil(W / 8)) of the partial layout. CTAs of 128 threads with
+// One warp per four (theta, eight-window group) items; grid covers ceil(N G / 4) warps, G =
+// ceil(W / 8) (the partial layout's window groups). CTAs of 128 threads with
 // kLaneParkBytes of dynamic shared memory. MINB sets the register cap (2: ~200, 3: 168, 4: 128);
 // shared memory holds every variant to three CTAs per SM, and at 128 registers the code still
 // needs no spills.
@@ -222,14 +229,11 @@ __global__ void __launch_bounds__(128, MINB) rollout_lane_kernel(const __grid_co
                                                                  float* __restrict__ partial,
                                                                  unsigned long long* __restrict__ n_bad) {
   extern __shared__ float4 lane_smem[];              // kLaneParkBytes
-  __shared__ BaseParams<float> bp_warp[4];
-  __shared__ float4 gains_warp[4][8];
-  const int WB = (win.W + 31) >> 5;
+  __shared__ BaseParams<float> bp_warp[4][4];
+  __shared__ float4 gains_warp[4][4][8];
   const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (warp >= (long long)N * WB) return;   // uniform per warp
-  const int n = (int)(warp / WB), wb = (int)(warp % WB);
-  rollout_lane_warp<MS>(M, win, theta + (size_t)n * SPI_THETA_DIM, wb, partial + (size_t)n * G * SPI_N_COMP,
-                                 G, n_bad, lane_smem, bp_warp, gains_warp);
+  if (warp * 4 >= (long long)N * G) return;   // uniform per warp
+  rollout_lane_warp<MS>(M, win, theta, warp * 4, N, partial, G, n_bad, lane_smem, bp_warp, gains_warp);
 }
 
 }  // namespace spi

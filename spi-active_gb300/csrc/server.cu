@@ -134,8 +134,8 @@ __global__ void __launch_bounds__(128, MINB) server_rollout_lane_kernel(const __
                                                                   unsigned long long* __restrict__ n_bad,
                                                                   int max_slots, int round) {
   extern __shared__ float4 lane_smem[];              // kLaneParkBytes
-  __shared__ BaseParams<float> bp_warp[4];
-  __shared__ float4 gains_warp[4][8];
+  __shared__ BaseParams<float> bp_warp[4][4];
+  __shared__ float4 gains_warp[4][4][8];
   const int lane = threadIdx.x & 31;
   const TickInfo* info = info_all + round;
   const int* order = order_all + (size_t)round * max_slots;
@@ -158,10 +158,8 @@ __global__ void __launch_bounds__(128, MINB) server_rollout_lane_kernel(const __
       }
       const SlotDesc& S = slots[order[lo]];
       const long long local = item - begin[order[lo]];
-      const int WB = (S.win.W + 31) >> 5;
-      const int n = (int)(local / WB), wb = (int)(local % WB);
-      rollout_lane_warp<MS>(M, S.win, S.theta + (size_t)n * SPI_THETA_DIM, wb,
-                               S.partial + (size_t)n * S.G * SPI_N_COMP, S.G, n_bad, lane_smem, bp_warp, gains_warp);
+      rollout_lane_warp<MS>(M, S.win, S.theta, local * 4, S.N, S.partial, S.G, n_bad, lane_smem, bp_warp,
+                            gains_warp);
     }
   }
 }
@@ -237,11 +235,11 @@ struct spi_server {
 
 namespace {
 
-// Work items of one slot per tick: (theta, 8-window group) in the quad layout, (theta, 32-window
-// block) in the lane layout.
+// Work items of one slot per tick: (theta, 8-window group) in the quad layout, four of them (a
+// warp's worth) in the lane layout.
 long long slot_items(const spi_server* s, const SlotDesc& d) {
-  const int per_theta = s->layout == SPI_LAYOUT_LANE ? (d.win.W + 31) / 32 : d.G;
-  return (long long)d.N * per_theta;
+  const long long groups = (long long)d.N * d.G;
+  return s->layout == SPI_LAYOUT_LANE ? (groups + 3) / 4 : groups;
 }
 
 bool server_busy(const spi_server* s) {
