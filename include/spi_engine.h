@@ -262,8 +262,8 @@ int spi_server_poll(spi_server* s, spi_job_result* results, int max, int32_t* n_
 int spi_server_wait(spi_server* s);
 /* Active job count and free budget. */
 int spi_server_stats(spi_server* s, int32_t* active, size_t* bytes_free);
-/* Cap on rollout work per tick, in work items (theta x 8-window group in the quad layout,
- * theta x 32-window block in the lane layout; 0 = no cap). Admission depends only on slots and
+/* Cap on rollout work per tick, in work items (one theta x 8-window group in the quad layout,
+ * four of them in the lane layout; 0 = no cap). Admission depends only on slots and
  * the HBM budget; each tick then runs the admitted jobs with the least remaining work
  * (remaining iterations x work items x horizon) first, as many as fit the cap (at least one),
  * and the others stay resident until they are among the shortest. Once the GPU is full,
@@ -276,7 +276,7 @@ int spi_server_config(spi_server* s, int ctas_per_sm, int items_per_claim);
  * 2 to 4 in the lane layout), as spi_set_kernel_config. */
 int spi_server_set_kernel_config(spi_server* s, int min_blocks);
 /* Rollout-kernel lane layout of the server: SPI_LAYOUT_QUAD (min_blocks 3 or 4) or
- * SPI_LAYOUT_LANE (one lane per rollout, work items of 32 windows; min_blocks 2 to 4), as
+ * SPI_LAYOUT_LANE (one lane per rollout, work items of four 8-window groups; min_blocks 2 to 4), as
  * spi_set_kernel_layout. Only while no job is held (SPI_ESTATE otherwise). */
 int spi_server_set_kernel_layout(spi_server* s, int layout);
 /* CEM-iteration rounds per tick (1..8, default 1). Each tick runs this many rounds of one

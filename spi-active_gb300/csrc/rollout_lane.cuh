@@ -1,8 +1,8 @@
 // rollout_lane.cuh -- lane-per-rollout layout of the rollout: one lane carries one (theta,
 // window) pair through all four legs.
 //
-// A warp evaluates one theta sample against 32 consecutive windows (four window groups of
-// eight). Per physics substep each lane runs phase A for legs FL, FR, RL, RR in turn, adding
+// A warp evaluates four (theta, eight-window group) items, one lane per window. Per physics
+// substep each lane runs phase A for legs FL, FR, RL, RR in turn, adding
 // their base contributions, solves the base once (phase B) and runs phase C for the four
 // legs. Compared with the quad layout (rollout.cuh) the base solve is not repeated on four
 // lanes and no shuffles combine the legs; the model is passed by value in the kernel's

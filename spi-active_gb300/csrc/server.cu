@@ -121,8 +121,8 @@ __global__ void __launch_bounds__(128, MINB) server_rollout_kernel(const DevMode
   }
 }
 
-// The same in the lane layout: each work item is one (slot, theta, 32-window block), one lane
-// per window through all four legs (rollout_lane_warp). CTAs of 128 threads with kLaneParkBytes
+// The same in the lane layout: each work item is four (theta, 8-window group) items of one slot,
+// one lane per window through all four legs (rollout_lane_warp). CTAs of 128 threads with kLaneParkBytes
 // of dynamic shared memory; the model by value; MS its motor shape.
 template <int MINB, int MS = kMotorRuntime>
 __global__ void __launch_bounds__(128, MINB) server_rollout_lane_kernel(const __grid_constant__ DevModel M,

@@ -5,8 +5,7 @@ each), "block" (the quad layout with each rollout's base solved once by one warp
 and "lane" (one lane per rollout through all four legs) -- and occupancy variants: the
 register allocator targets 2..5 CTAs of 128 threads per SM (255 / 168 / 128 / 96 registers
 per thread, with more spilling as registers shrink). Which is fastest depends on the
-horizon, the window count (the lane layout fills warps in blocks of 32 windows, the quad
-layout in groups of 8) and the GPU, so the variant is picked by timing each on the caller's
+horizon, the window count and the GPU, so the variant is picked by timing each on the caller's
 own windows and theta batch. Choices are cached per (GPU, horizon bucket, work bucket,
 window-count remainder) in the build folder.
 """
