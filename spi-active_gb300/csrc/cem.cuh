@@ -146,20 +146,46 @@ static __global__ void __launch_bounds__(1024) cem_refit_kernel(CemState* __rest
     if (lane == 0) s_mu[d] = s / ne;
   }
   __syncthreads();
-  // elite covariance, one warp per upper-triangle entry
+  // elite covariance, one warp per upper-triangle entry (three entries a warp at most: P <= 13
+  // gives at most 91 entries for 32 warps). The elite rows are centred once, kEliteChunk at a
+  // time, in shared memory (FP64 work is scarce); each lane still sums its elites e = lane,
+  // lane + 32, ... in order, so the result equals a pass over the unstaged rows.
+  constexpr int kEliteChunk = 256;   // a multiple of 32
+  __shared__ double s_c[kEliteChunk * CEM_MAX_DIM];
   const int nent = P * (P + 1) / 2;
-  for (int q = warp; q < nent; q += nwarps) {
-    int i = 0, r = q;
-    while (r >= P - i) { r -= P - i; ++i; }
-    const int j = i + r;
-    const int si = st->param_ids[i], sj = st->param_ids[j];
-    double s = 0.0;
-    for (int e = lane; e < ne; e += 32) {
-      const float* t = theta + (size_t)(keys[e] & 0xFFFFFFFFull) * SPI_THETA_DIM;
-      s += ((double)t[si] - s_mu[i]) * ((double)t[sj] - s_mu[j]);
+  double acc[3] = {0.0, 0.0, 0.0};
+  for (int e0 = 0; e0 < ne; e0 += kEliteChunk) {
+    const int m = min(kEliteChunk, ne - e0);
+    __syncthreads();                  // the previous chunk has been read
+    for (int t = threadIdx.x; t < m * P; t += blockDim.x) {
+      const int e = t / P, d = t % P;
+      s_c[e * CEM_MAX_DIM + d] =
+          (double)theta[(size_t)(keys[e0 + e] & 0xFFFFFFFFull) * SPI_THETA_DIM + st->param_ids[d]] - s_mu[d];
     }
-    s = warp_sum_d(s);
-    if (lane == 0) { s_cov[i * CEM_MAX_DIM + j] = s / ne; s_cov[j * CEM_MAX_DIM + i] = s / ne; }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const int q = warp + k * nwarps;
+      if (q < nent) {
+        int i = 0, r = q;
+        while (r >= P - i) { r -= P - i; ++i; }
+        const int j = i + r;
+        double s = acc[k];
+        for (int e = lane; e < m; e += 32) s += s_c[e * CEM_MAX_DIM + i] * s_c[e * CEM_MAX_DIM + j];
+        acc[k] = s;
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const int q = warp + k * nwarps;
+    if (q < nent) {
+      int i = 0, r = q;
+      while (r >= P - i) { r -= P - i; ++i; }
+      const int j = i + r;
+      const double s = warp_sum_d(acc[k]);
+      if (lane == 0) { s_cov[i * CEM_MAX_DIM + j] = s / ne; s_cov[j * CEM_MAX_DIM + i] = s / ne; }
+    }
   }
   __syncthreads();
   // smoothed mean and covariance (+ the std floor on the diagonal), element-parallel, kept in
