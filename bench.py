@@ -11,8 +11,10 @@ elite refit + resampling, all on the device.
 
 ``--impl reference`` times the reference path's CPU restatement (the FP64 NumPy
 oracle; Isaac Gym cannot be installed) on the host cores on a bounded sample of the
-same workload. Under torchrun (N > 1) every rank runs an independent replica job
-(the path has no cross-job exchange); rank 0 prints.
+same workload. With N > 1 every rank runs an independent replica job (the path has no
+cross-job exchange) and rank 0 prints; ``--gpus N`` started as a plain process relaunches
+itself under torch.distributed.run with N ranks. ``--launch-check`` runs only that replica
+plumbing (ranks, barrier, slowest-rank time) on a fixed host workload, without a GPU.
 """
 from __future__ import annotations
 
@@ -46,7 +48,12 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", choices=("c1", "c2", "c3", "c4"), default="c1")
+    ap.add_argument("--workload", choices=("c1", "c2", "c3", "c4", "rollout-case"), default="c1")
+    ap.add_argument("--variant", default="lane4", help="rollout-case: rollout-kernel variant")
+    ap.add_argument("--n-theta", type=int, default=1024, help="rollout-case: theta samples")
+    ap.add_argument("--n-windows", type=int, default=256, help="rollout-case: windows")
+    ap.add_argument("--horizon", type=int, default=20, help="rollout-case: control steps per window")
+    ap.add_argument("--runs", type=int, default=3, help="rollout-case: launches, the last one timed")
     ap.add_argument("--c3-candidates", type=int, default=512, help="c3: candidate excitations scored per step")
     ap.add_argument("--no-serving", action="store_true", help="c1: skip the served-vs-plain job mix")
     ap.add_argument("--mix-jobs", type=int, default=16, help="c1: jobs in the served-vs-plain mix")
@@ -55,7 +62,46 @@ def parse_args():
     ap.add_argument("--c4-rate", type=float, default=200.0, help="c4: arrivals per second")
     ap.add_argument("--c4-jobs", type=int, default=64, help="c4: jobs in the stream")
     ap.add_argument("--iters", type=int, default=30, help="c2/c4: CEM iterations per job")
+    ap.add_argument("--launch-check", action="store_true",
+                    help="replica launch plumbing only: a fixed host workload per rank, no GPU, no rollouts")
     return ap.parse_args()
+
+
+def relaunch_under_torchrun(n: int) -> int:
+    """Start this script again as n ranks of one node (torch.distributed.run on 127.0.0.1)."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr=127.0.0.1", f"--master-port={port}", str(Path(__file__).resolve()), *sys.argv[1:]]
+    return subprocess.run(cmd).returncode
+
+
+def run_launch_check(args):
+    """Each rank times the same fixed host workload (a seeded 256 x 256 FP64 matrix power); the
+    line reports the whole-job rate over the slowest rank, as the GPU replica path does."""
+    from spi_gb300 import replicas
+    r = replicas.init("gloo")
+    a = np.random.default_rng(r.rank).random((256, 256)) / 256.0
+    for _ in range(args.warmup):
+        a @ a
+    r.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        b = a
+        for _ in range(8):
+            b = b @ a
+    local_ms = (time.perf_counter() - t0) * 1e3
+    value, ms = r.whole_job_rate(8.0 * args.steps, local_ms)
+    if r.rank == 0:
+        print(json.dumps({"metric": "matrix products/s (launch check, no rollouts)", "value": value,
+                          "unit": "products/s", "n_gpus": r.world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": ms / max(args.steps, 1), "higher_is_better": True, "scaling": "weak",
+                          "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                          "config": {"workload": "launch check: replica ranks over gloo, host workload only"},
+                          "slowest_rank_ms": ms}), flush=True)
+    r.close()
 
 
 # --------------------------------------------------------------------------------------
@@ -292,6 +338,97 @@ def run_c3(args):
     print(json.dumps(line), flush=True)
 
 
+def recorded_dram_bytes(kernel: str):
+    """(dram__bytes_read.sum + dram__bytes_write.sum per launch, the ncu command) from the
+    kernel's recorded capture on 1024 theta x 256 windows x H=20, or (None, None) without one."""
+    rec = ROOT / "profiles" / f"{kernel}_1024x256xH20_dram.txt"
+    if not rec.exists():
+        return None, None
+    vals, cmd = {}, None
+    for ln in rec.read_text().splitlines():
+        f = ln.split()
+        if ln.startswith("command:"):
+            cmd = ln[len("command:"):].strip()
+        elif len(f) == 2 and f[0] in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+            vals[f[0]] = int(f[1])
+    if len(vals) != 2:
+        return None, None
+    return vals["dram__bytes_read.sum"] + vals["dram__bytes_write.sum"], cmd
+
+
+def identification_report(cem, eng, theta_true):
+    """Per-parameter result of the CEM identification, and which parameters the excitation
+    leaves unidentified. The information check: F = sum_w J_w^T Q J_w at the true theta over
+    the loaded windows (forward-mode sensitivities, Q the cost's state weights); for each
+    parameter sqrt((F^-1)_ii) / (hi - lo) is the cost-curvature std in units of its prior range,
+    so a large value means the windows barely constrain that parameter."""
+    import torch
+    from spi_gb300.engine import DEFAULT_SQ_WEIGHTS
+    from spi_gb300.robot import THETA_NAMES
+    from spi_gb300.sensitivity import block_weights, sensitivities
+    te = cem.theta_errors(theta_true)
+    J, _ = sensitivities(eng, np.asarray(theta_true, np.float32)[None], cem.param_ids)
+    q = torch.as_tensor(block_weights(DEFAULT_SQ_WEIGHTS), device=J.device, dtype=torch.float64)
+    Jd = J[0].double()                                             # [W, 37, K]
+    F = torch.einsum("wik,i,wil->kl", Jd, q, Jd).cpu().numpy() / J.shape[1]
+    rng = cem.hi - cem.lo
+    Fs = F * np.outer(rng, rng)                                    # in prior-range units
+    crlb = np.sqrt(np.maximum(np.diag(np.linalg.pinv(Fs + 1e-12 * np.trace(Fs) * np.eye(len(rng)))), 0.0))
+    names = [THETA_NAMES[i] for i in cem.param_ids]
+    per = {n: {"true": float(t), "est": float(e), "err_frac": float(ef), "std_frac": float(sf),
+               "info_std_frac": float(c)}
+           for n, t, e, ef, sf, c in zip(names, te["true"], te["est"], te["err_frac"], te["std_frac"], crlb)}
+    worst = int(np.argmax(te["err_frac"]))
+    return {"best_cost": cem.best_cost(), "theta_err": float(te["err_frac"][worst]), "theta_err_param": names[worst],
+            "per_param": per,
+            "not_identified": [n for n, ef in zip(names, te["err_frac"]) if ef > 0.1],
+            "note": "err_frac = |CEM mean - truth| / prior range; info_std_frac = sqrt((F^-1)_ii) / prior range "
+                    "from the exact Fisher information of the cost at the truth over the 256 windows"}
+
+
+def run_rollout_case(args):
+    """One rollout-kernel case for profilers: ground-truth windows generated on the GPU (one
+    trace-kernel launch), prior theta samples, `--runs` launches of spi_run with the chosen
+    variant, the last one timed with CUDA events. Under ncu, skip the first runs - 1 launches of
+    the kernel with -s and capture one with -c 1."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from spi_gb300 import robot
+    from spi_gb300.autotune import set_variant
+    from spi_gb300.data import synthetic_windows
+    from spi_gb300.engine import Engine
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(5)
+    lo, hi = robot.THETA_PRIOR_LO, robot.THETA_PRIOR_HI
+    e = Engine()
+    init, act, tgt = synthetic_windows(e, lo + (hi - lo) * rng.random(13), args.n_windows, args.horizon, seed=77)
+    e.load_windows(torch.from_numpy(init), torch.from_numpy(act), torch.from_numpy(tgt))
+    e.set_theta(torch.from_numpy((lo + (hi - lo) * rng.random((args.n_theta, 13))).astype(np.float32)))
+    set_variant(e, args.variant)
+    for _ in range(args.runs - 1):
+        e.run()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record(e.stream)
+    e.run()
+    t1.record(e.stream)
+    t1.synchronize()
+    _, cost = e.read()
+    torch.cuda.synchronize()
+    n_bad = e.sync()
+    if n_bad:
+        raise SystemExit(f"{n_bad} non-finite rollouts")
+    ms = t0.elapsed_time(t1)
+    steps = args.n_theta * args.n_windows * args.horizon
+    print(json.dumps({"metric": METRIC, "value": steps / (ms * 1e-3), "unit": METRIC, "n_gpus": 1, "steps": 1,
+                      "warmup": args.runs - 1, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                      "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                      "config": {"workload": f"rollout-case: {args.n_theta} theta x {args.n_windows} windows x "
+                                             f"H={args.horizon}, one spi_run launch timed",
+                                 "kernel_variant": args.variant},
+                      "median_cost": float(cost.median())}), flush=True)
+
+
 def run_reference(args):
     """The reference arm: the FP64 oracle (the reference path's CPU restatement) on all host
     cores, W warm-up steps then K timed steps. One step is a bounded sample of the C1 workload:
@@ -428,14 +565,15 @@ def run_ours(args):
     kmean = float(np.mean(kern_ms))
     peak = probe_fp32_peak()
     achieved = steps_per_iter * fl / (kmean * 1e-3)
+    kname = {"lane": "rollout_lane_kernel", "bloc": "rollout_block_kernel"}.get(variant[:4], "rollout_kernel")
+    traffic, traffic_cmd = recorded_dram_bytes(kname)
     roof = {"bound": "fp32", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": 418304 if variant.startswith("lane") else 419328,
-            "traffic_note": "dram read+write bytes per launch from ncu on 1024 theta x the same 256 windows "
-                            "(profiles/rollout_lane_kernel_1024x256xH20.md, rollout_kernel_1024x256xH20_full.md); "
-                            "the window set is read once and theta / partials stay in L2, so traffic does not "
-                            "scale with theta",
-            "kernel": {"lane": "rollout_lane_kernel", "bloc": "rollout_block_kernel"}.get(variant[:4], "rollout_kernel")
-                      + " (+finalize_costs)",
+            "frac": achieved / peak, "traffic": traffic,
+            "traffic_note": "dram read+write bytes per launch, recorded from one ncu capture of the kernel on "
+                            "1024 theta x the same 256 windows x H=20 (" + (traffic_cmd or "no record") + "); the "
+                            "window set is read once and theta / partials stay in L2, so traffic does not scale "
+                            "with theta",
+            "kernel": kname + " (+finalize_costs)",
             "kernel_ms": kmean,
             "flops_per_rollout_step": fl,
             "flops_note": "algorithmic count: the oracle's equations (legs by the articulated-body algorithm), "
@@ -456,7 +594,7 @@ def run_ours(args):
                        "kernel_variant": {"chosen": variant, "tuning_ms": variant_ms}},
             "roofline": roof, "e2e": e2e, "gpu_launches": cem.launches_per_step * args.steps,
             "wall_s": wall, "nonfinite_rollouts": n_bad, "clocks": clocks.summary(),
-            "cem": {"best_cost": cem.best_cost(), "theta_err": cem.theta_error(theta_true)}}
+            "cem": identification_report(cem, eng, theta_true)}
     if ws == 1 and not args.no_serving:
         from spi_gb300.workloads import c2_specs, small_specs
         from spi_gb300.server import Server
@@ -477,10 +615,16 @@ def run_ours(args):
 
 def main():
     args = parse_args()
-    if args.impl == "reference":
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(relaunch_under_torchrun(args.gpus))
+    if args.launch_check:
+        run_launch_check(args)
+    elif args.impl == "reference":
         run_reference(args)
     elif args.workload == "c3":
         run_c3(args)
+    elif args.workload == "rollout-case":
+        run_rollout_case(args)
     elif args.workload in ("c2", "c4"):
         run_multijob(args)
     else:

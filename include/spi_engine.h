@@ -297,7 +297,10 @@ int spi_server_set_rounds(spi_server* s, int rounds);
  * GPU loading the library keeps until exit: N * ceil(W / 8) <= SPI_NOALLOC_MAX_GROUPS, larger
  * requests fail with SPI_EINVAL. All calls share that array, so calls that overlap on the GPU
  * race; serialise them. The first call on a device looks up the array's address on that
- * device; make it before any stream capture. Asynchronous on `stream` (a cudaStream_t). */
+ * device; make it before any stream capture. Asynchronous on `stream` (a cudaStream_t).
+ * Unlike spi_run, it counts no non-finite rollouts (there is no spi_sync counter behind it): a
+ * rollout whose final state is not finite shows up as non-finite entries in that theta's row of
+ * comp, so callers check comp (or cost) for NaN / inf themselves. */
 #define SPI_NOALLOC_MAX_GROUPS 65536
 int spi_eval_windows_noalloc(const spi_robot* robot, const float* init, const float* actions,
                              const float* target, const float* weight, int W, int H, float norm,

@@ -19,13 +19,19 @@
 // earlier call are never summed. The first call on a device resolves the array's device
 // address with cudaGetSymbolAddress (with that device current); make that first call
 // before any stream capture.
+//
+// Non-finite rollouts: spi_run counts rollouts whose final state is not finite (read with
+// spi_sync); this entry point keeps no such count, since a counter would be one more piece of
+// device memory. A non-finite final state reaches the outputs instead: every error component
+// of that window is summed (with weight 0 too, as 0 * NaN is NaN), so the theta's row of comp
+// turns non-finite. Callers check comp (or the cost) themselves.
 #include <cuda_runtime.h>
 
 #include <mutex>
 
 #include "common.h"
-#include "dynamics.cuh"
 #include "model.h"
+#include "rollout.cuh"
 
 using namespace spi;
 
@@ -39,30 +45,6 @@ static __device__ __align__(256) float g_partials[(size_t)kMaxGroups * SPI_N_COM
 
 std::mutex g_mu;
 float* g_partials_addr[kMaxDevices] = {nullptr};
-
-__device__ __forceinline__ float nq_sum(float x) {
-  x += __shfl_xor_sync(0xffffffffu, x, 1);
-  x += __shfl_xor_sync(0xffffffffu, x, 2);
-  return x;
-}
-__device__ __forceinline__ float nslot_sum(float x) {
-  x += __shfl_xor_sync(0xffffffffu, x, 4);
-  x += __shfl_xor_sync(0xffffffffu, x, 8);
-  x += __shfl_xor_sync(0xffffffffu, x, 16);
-  return x;
-}
-__device__ __forceinline__ void nq_sum_out(LegOut<float>& o) {
-  o.I.A.xx = nq_sum(o.I.A.xx); o.I.A.yy = nq_sum(o.I.A.yy); o.I.A.zz = nq_sum(o.I.A.zz);
-  o.I.A.xy = nq_sum(o.I.A.xy); o.I.A.xz = nq_sum(o.I.A.xz); o.I.A.yz = nq_sum(o.I.A.yz);
-  o.I.C.xx = nq_sum(o.I.C.xx); o.I.C.yy = nq_sum(o.I.C.yy); o.I.C.zz = nq_sum(o.I.C.zz);
-  o.I.C.xy = nq_sum(o.I.C.xy); o.I.C.xz = nq_sum(o.I.C.xz); o.I.C.yz = nq_sum(o.I.C.yz);
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j) o.I.B.m[i][j] = nq_sum(o.I.B.m[i][j]);
-  o.p.w.x = nq_sum(o.p.w.x); o.p.w.y = nq_sum(o.p.w.y); o.p.w.z = nq_sum(o.p.w.z);
-  o.p.v.x = nq_sum(o.p.v.x); o.p.v.y = nq_sum(o.p.v.y); o.p.v.z = nq_sum(o.p.v.z);
-}
 
 // One warp per (theta n, window group g): 8 windows, 4 lanes (legs) per window.
 __global__ void __launch_bounds__(128) rollout_rows_kernel(const DevModel model, const float* __restrict__ init,
@@ -108,13 +90,7 @@ __global__ void __launch_bounds__(128) rollout_rows_kernel(const DevModel model,
   for (int h = 0; h < H; ++h) {
     const float* ap = actions + ((size_t)w * H + h) * 12 + 3 * leg;
     float act[3] = {__ldg(ap), __ldg(ap + 1), __ldg(ap + 2)};
-    for (int s = 0; s < M.decimation; ++s) {
-      LegWork<float> lw;
-      LegOut<float> o = phase_a(M, leg, B, L, lp, act, lw);
-      nq_sum_out(o);
-      SV<float> a0 = phase_b(M, bp, o, B);
-      phase_c(M, leg, a0, lw, L);
-    }
+    for (int s = 0; s < M.decimation; ++s) substep(M, leg, B, L, bp, lp, act);
   }
   const float* tg = target + (size_t)w * SPI_STATE_DIM;
   float s13[13];
@@ -134,40 +110,27 @@ __global__ void __launch_bounds__(128) rollout_rows_kernel(const DevModel model,
     sj += dq * dq;
     sjd += dqd * dqd;
   }
-  sp = nq_sum(sp); sq = nq_sum(sq); sv = nq_sum(sv); sw = nq_sum(sw); sj = nq_sum(sj); sjd = nq_sum(sjd);
+  sp = qsum(sp); sq = qsum(sq); sv = qsum(sv); sw = qsum(sw); sj = qsum(sj); sjd = qsum(sjd);
   const float wt = active ? (weight ? __ldg(weight + w) : 1.0f) : 0.f;
   const float comp[SPI_N_COMP] = {sqrtf(sp), sqrtf(sq), sqrtf(sj), sp, sq, sv, sw, sj, sjd};
   float* out = partials + ((size_t)n * G + g) * SPI_N_COMP;
 #pragma unroll
   for (int k = 0; k < SPI_N_COMP; ++k) {
-    const float v = nslot_sum(active ? comp[k] * wt : 0.f);
+    const float v = slot_sum(active ? comp[k] * wt : 0.f);
     if (lane == 0) out[k] = v;
   }
 }
 
+// The engine's finalize (rollout.cuh finalize_one): partials summed in group order, the
+// weighted cost formed with the same pinned roundings, so both paths give the same costs
+// from the same partials.
 __global__ void finalize_rows_kernel(const float* __restrict__ partials, int N, int G, float norm, int mode,
                                      float w0, float w1, float w2, float w3, float w4, float w5,
                                      float* __restrict__ comp, float* __restrict__ cost) {
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= N) return;
-  float c[SPI_N_COMP];
-#pragma unroll
-  for (int k = 0; k < SPI_N_COMP; ++k) c[k] = 0.f;
-  for (int g = 0; g < G; ++g) {
-#pragma unroll
-    for (int k = 0; k < SPI_N_COMP; ++k) c[k] += partials[((size_t)n * G + g) * SPI_N_COMP + k];
-  }
-  const float inv = 1.0f / norm;
-#pragma unroll
-  for (int k = 0; k < SPI_N_COMP; ++k) c[k] *= inv;
-  if (comp) {
-#pragma unroll
-    for (int k = 0; k < SPI_N_COMP; ++k) comp[(size_t)n * SPI_N_COMP + k] = c[k];
-  }
-  if (cost) {
-    cost[n] = mode == 0 ? 10.f * c[0] + 5.f * c[1] + 1.f * c[2]
-                        : w0 * c[3] + w1 * c[4] + w2 * c[5] + w3 * c[6] + w4 * c[7] + w5 * c[8];
-  }
+  const float w[6] = {w0, w1, w2, w3, w4, w5};
+  finalize_one(partials, n, G, norm, mode, w, comp, cost);
 }
 
 // Device address of g_partials on the current device, resolved once per device.

@@ -113,10 +113,18 @@ class CEM:
         return self.read()["best_cost"]
 
     def theta_error(self, theta_true):
+        """Largest |mean - truth| over the identified parameters, in units of each prior range."""
+        return float(np.max(self.theta_errors(theta_true)["err_frac"]))
+
+    def theta_errors(self, theta_true):
+        """Per identified parameter: truth, distribution mean, |mean - truth| and the
+        distribution's std, the last two in units of the parameter's prior range (hi - lo)."""
         r = self.read()
         est = np.array(r["mu"])
         true = np.asarray(theta_true, np.float64)[self.param_ids]
-        return float(np.max(np.abs(est - true) / (self.hi - self.lo)))
+        rng = self.hi - self.lo
+        return {"true": true, "est": est, "err_frac": np.abs(est - true) / rng,
+                "std_frac": np.sqrt(np.maximum(np.diag(r["cov"]), 0.0)) / rng}
 
     def sample_host(self, k):
         """k host-side uniform prior populations (for end-to-end host-buffer timing)."""

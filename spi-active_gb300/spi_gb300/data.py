@@ -13,7 +13,8 @@
 * ``collect`` rolls trajectories on the GPU engine (the counterpart of the
   Isaac Gym collectors scripts/data/{sine,jump,stand}.py), with per-joint sine
   targets, the synchronized thigh/calf sine of sine.py:39-45 / jump.py:15-21
-  or zero actions (stand.py).
+  or zero actions (stand.py); ``collect_profile`` runs one of the reference's
+  three profiles end to end and returns its npz dict.
 """
 from __future__ import annotations
 
@@ -56,6 +57,37 @@ def reference_sine_actions(T, amplitude, frequency, control_dt) -> np.ndarray:
     a[0][:, list(THIGH_IDX)] = phase[:, None]
     a[0][:, list(CALF_IDX)] = -phase[:, None]
     return a
+
+
+# Open-loop profiles of the reference's collectors: thigh targets +A sin(2 pi f t), calf targets
+# -A sin(2 pi f t) in action units, 5 s from a base height of 0.32 m (scripts/data/sine.py:15-21,
+# 39-45; jump.py:15-21, 39-45), or zero actions (stand.py:14-15, 21).
+PROFILES = {"sine": (0.8, 1.0), "jump": (1.2, 1.5), "stand": (0.0, 0.0)}
+COLLECT_DURATION_S = 5.0
+COLLECT_BASE_HEIGHT = 0.32
+
+
+def profile_actions(profile: str, T: int, control_dt: float) -> np.ndarray:
+    """Actions [1, T, 12] of a reference collector profile ("sine", "jump" or "stand")."""
+    if profile not in PROFILES:
+        raise ValueError(f"unknown collector profile {profile!r} (one of {sorted(PROFILES)})")
+    amp, freq = PROFILES[profile]
+    return reference_sine_actions(T, amp, freq, control_dt)
+
+
+def collect_profile(engine, profile: str, duration_s: float = COLLECT_DURATION_S, theta=None,
+                    base_height: float = COLLECT_BASE_HEIGHT) -> dict:
+    """One trajectory of a reference collector profile rolled on the GPU engine, as the npz dict
+    the reference's collectors write (states after each action, the action, PD gains)."""
+    from .robot import THETA_NOMINAL
+    cfg = engine.cfg
+    T = int(round(duration_s / cfg.control_dt))
+    if T <= 0:
+        raise ValueError(f"duration {duration_s} s is shorter than one control step")
+    acts = profile_actions(profile, T, cfg.control_dt)
+    th = THETA_NOMINAL if theta is None else theta
+    states = collect(engine, standing_state(1, z=base_height), acts, th)
+    return format_data(states[0], acts[0], cfg)
 
 
 def collect(engine, x0, actions, theta) -> np.ndarray:

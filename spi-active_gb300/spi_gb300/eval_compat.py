@@ -13,11 +13,20 @@ Same names, arguments and results as the reference:
 * ``compute_cost(costs)``                          scripts/mass_opt.py:62-76
 * ``mass_sweep(env, dataset, H, masses, scales)``  scripts/mass_landscape.py:111-128
 
-``evaluate_batch`` reproduces the reference's chunked masking: windows at and
-after the first motion end of each ``num_envs`` chunk get weight 0, sums are
-divided by the number of non-end windows. The environment is the GPU engine: all
-windows of all chunks are rolled in one launch. ``mass_sweep`` evaluates every
-mass scale in the same launch instead of one scale after another.
+``evaluate_batch`` reproduces the reference's chunked evaluation:
+
+* windows at and after the first motion end of each ``num_envs`` chunk get
+  weight 0, and sums are divided by the number of non-end windows
+  (scripts/eval.py:279-280, 304-310);
+* each chunk runs with the PD gains of its first window, the row that
+  ``apply_pd_gains_batch`` takes from the chunk (scripts/eval.py:243-250), so a
+  dataset concatenated from files logged with different gains is scored with
+  each file's own gains.
+
+The environment is the GPU engine. Chunks that share a gain set are rolled in one
+launch (one engine per distinct gain set, all its windows at once), and the
+weighted sums of the gain groups add up to the reference's totals. ``mass_sweep``
+evaluates every mass scale in the same launches instead of one scale after another.
 """
 from __future__ import annotations
 
@@ -92,42 +101,64 @@ class EngineSimulatorHandle:
         self.body_masses = np.asarray(masses, dtype=np.float32)
 
 
+def chunk_gains(kp, kd, batch_size: int):
+    """Per-window PD gains as the reference's evaluate_batch applies them: every window of a
+    ``batch_size`` chunk runs with the chunk's first row (scripts/eval.py:243-250 with
+    apply_pd_gains_batch :192-201). kp, kd [W, 12] -> two [W, 12] float32 arrays."""
+    kp = np.asarray(kp, dtype=np.float32).reshape(len(kp), -1)
+    kd = np.asarray(kd, dtype=np.float32).reshape(len(kd), -1)
+    W = kp.shape[0]
+    first = (np.arange(W) // int(batch_size)) * int(batch_size)
+    return kp[first], kd[first]
+
+
 class EvalEnv:
-    """Stands in for the LeggedRobotBase that ``instantiate_env`` returns in the reference."""
+    """Stands in for the LeggedRobotBase that ``instantiate_env`` returns in the reference.
+
+    One GPU engine per distinct PD-gain set (the gains are part of the engine's robot model);
+    ``load`` splits a dataset's windows into gain groups by the reference's chunk rule."""
 
     def __init__(self, num_envs: int, cfg: SimConfig | None = None, device=None):
         self.num_envs = int(num_envs)
         self.dim_actions = 12
         self.cfg = cfg or SimConfig.reference_compatible()
         self.device = torch.device(device) if device is not None else torch.device("cuda")
-        self.engine = Engine(self.cfg, device=self.device)
-        self.engine.set_cost(COST_REF)
+        self._engines: dict = {}
         self.simulator = EngineSimulatorHandle(self)
         self.theta = torch.tensor(THETA_NOMINAL, dtype=torch.float32, device=self.device)[None].clone()
         self._loaded = None
+        self._groups = []
         self.p_gains = torch.tensor(np.broadcast_to(np.asarray(self.cfg.kp, np.float32), (12,)).copy(),
                                     device=self.device)
         self.d_gains = torch.tensor(np.broadcast_to(np.asarray(self.cfg.kd, np.float32), (12,)).copy(),
                                     device=self.device)
 
-    def _sync_gains(self):
-        kp = self.p_gains.detach().cpu().numpy().astype(np.float64)
-        kd = self.d_gains.detach().cpu().numpy().astype(np.float64)
-        if not (np.array_equal(np.broadcast_to(np.asarray(self.cfg.kp, np.float64), (12,)), kp)
-                and np.array_equal(np.broadcast_to(np.asarray(self.cfg.kd, np.float64), (12,)), kd)):
-            self.cfg = SimConfig(**{**self.cfg.__dict__, "kp": tuple(kp), "kd": tuple(kd)})
-            self.engine = Engine(self.cfg, device=self.device)
-            self.engine.set_cost(COST_REF)
-            self._loaded = None
+    def engine_for(self, kp, kd) -> Engine:
+        """The engine whose robot model carries these per-joint gains (created once per gain set)."""
+        key = (tuple(float(v) for v in np.broadcast_to(np.asarray(kp, np.float32), (12,))),
+               tuple(float(v) for v in np.broadcast_to(np.asarray(kd, np.float32), (12,))))
+        eng = self._engines.get(key)
+        if eng is None:
+            cfg = SimConfig(**{**self.cfg.__dict__, "kp": key[0], "kd": key[1]})
+            eng = Engine(cfg, device=self.device)
+            eng.set_cost(COST_REF)
+            self._engines[key] = eng
+        return eng
+
+    @property
+    def engine(self) -> Engine:
+        """The engine of the environment's current gains (p_gains / d_gains)."""
+        return self.engine_for(self.p_gains.detach().cpu().numpy(), self.d_gains.detach().cpu().numpy())
 
     def load(self, dataset: DatasetBatch):
-        self._sync_gains()
         key = (id(dataset), self.num_envs)
         if self._loaded == key:
             return
         me = dataset.motion_ends.detach().cpu().numpy()
         weight, n_valid = sd.eval_weights(me, self.num_envs)
         W = me.shape[0]
+        kp, kd = chunk_gains(dataset.pd_gain_kp.detach().cpu().numpy(),
+                             dataset.pd_gain_kd.detach().cpu().numpy(), self.num_envs)
         z3 = torch.zeros((W, 3), device=self.device)
         z12 = torch.zeros((W, 12), device=self.device)
         init = torch.cat([dataset.init_base_pos, dataset.init_base_ori, dataset.init_base_lin_vel,
@@ -137,14 +168,34 @@ class EvalEnv:
                          dataset.target_base_ang_vel if dataset.target_base_ang_vel is not None else z3,
                          dataset.target_joint_pos,
                          dataset.target_joint_vel if dataset.target_joint_vel is not None else z12], -1)
-        self.engine.load_windows(init, dataset.action_sequences, tgt, torch.from_numpy(weight), norm=n_valid)
+        gains = np.concatenate([kp, kd], 1)
+        _, group_of = np.unique(gains, axis=0, return_inverse=True)
+        group_of = group_of.reshape(-1)
+        self._groups = []
+        for gid in range(int(group_of.max()) + 1):
+            rows = np.flatnonzero(group_of == gid)
+            if not np.any(weight[rows] > 0):
+                continue                     # every window of this gain set is masked out
+            eng = self.engine_for(kp[rows[0]], kd[rows[0]])
+            idx = torch.from_numpy(rows).to(self.device)
+            eng.load_windows(init.index_select(0, idx), dataset.action_sequences.index_select(0, idx),
+                             tgt.index_select(0, idx), torch.from_numpy(weight[rows]), norm=n_valid)
+            self._groups.append(eng)
+        # the reference leaves the last chunk's gains applied
+        last = ((W - 1) // self.num_envs) * self.num_envs
+        self.p_gains[:] = torch.from_numpy(kp[last])
+        self.d_gains[:] = torch.from_numpy(kd[last])
         self._loaded = key
 
     def evaluate_thetas(self, dataset: DatasetBatch, theta: torch.Tensor) -> np.ndarray:
-        """Reference (base_pos, base_quat, joint_pos) means for every row of theta [N,13]."""
+        """Reference (base_pos, base_quat, joint_pos) means for every row of theta [N,13]: the
+        weighted sums of every gain group over the dataset's non-end window count."""
         self.load(dataset)
-        comp, _ = self.engine.evaluate(theta)
-        return comp[:, 0:3].double().cpu().numpy()
+        total = np.zeros((int(theta.shape[0]), 3))
+        for eng in self._groups:
+            comp, _ = eng.evaluate(theta)
+            total += comp[:, 0:3].double().cpu().numpy()
+        return total
 
 
 def instantiate_env(base_dir=None, num_envs: int = 4096, config_name: str = "env/go2_test", seed: int = 0,
@@ -157,6 +208,8 @@ def capture_reference_masses(simulator) -> np.ndarray:
 
 
 def apply_pd_gains_batch(env: EvalEnv, kp_batch: torch.Tensor, kd_batch: torch.Tensor) -> None:
+    """The env's current gains become the batch's first row (``env.engine`` then runs with them).
+    evaluate_batch applies each chunk's own first row itself."""
     env.p_gains[:] = kp_batch[0]
     env.d_gains[:] = kd_batch[0]
 
@@ -169,7 +222,6 @@ def apply_base_mass(simulator, reference_masses: np.ndarray, base_mass: float) -
 def evaluate_batch(env: EvalEnv, horizon: int, action_buffer: torch.Tensor, dataset: DatasetBatch) -> MassEvalResult:
     if dataset.action_sequences.shape[1] != horizon:
         raise ValueError(f"dataset horizon {dataset.action_sequences.shape[1]} != {horizon}")
-    apply_pd_gains_batch(env, dataset.pd_gain_kp, dataset.pd_gain_kd)
     r = env.evaluate_thetas(dataset, env.theta)[0]
     return MassEvalResult(base_pos=float(r[0]), base_quat=float(r[1]), joint_pos=float(r[2]))
 
@@ -187,5 +239,4 @@ def mass_sweep(env: EvalEnv, dataset: DatasetBatch, horizon: int, reference_mass
     base_nominal = float(reference_masses[0])
     theta = env.theta.repeat(len(scales), 1)
     theta[:, 0] = torch.from_numpy((base_nominal * scales.astype(np.float64)).astype(np.float32)).to(theta.device)
-    apply_pd_gains_batch(env, dataset.pd_gain_kp, dataset.pd_gain_kd)
     return env.evaluate_thetas(dataset, theta).astype(np.float32)

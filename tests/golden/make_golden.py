@@ -1,9 +1,8 @@
 """Generate the golden vectors in this folder by executing the reference's own code.
 
-Run where the reference checkout exists (``SPI_REFERENCE``, default
-``/root/reference``)::
+Run where a reference checkout exists, naming it in ``SPI_REFERENCE``::
 
-    PYTHONPATH=. python tests/golden/make_golden.py
+    SPI_REFERENCE=<path of the reference checkout> PYTHONPATH=. python tests/golden/make_golden.py
 
 The reference cannot be imported whole (Isaac Gym, Hydra and Optuna are not
 installable), so each function below is pulled out of its source file with
@@ -19,7 +18,8 @@ Pinned functions (reference file:line):
 * ActiveSysId_OpenLoop.act2tau_scalar / act2tau_vec3 / act2tau_vec3_tanh /
   _reward_fisher_information_matrix  spigym/envs/sysid/active_sysid_openloop.py:356-426
 * load_dataset / to_device / capture_reference_masses / apply_pd_gains_batch /
-  apply_base_mass / evaluate_batch  scripts/eval.py:101-310
+  apply_base_mass / evaluate_batch  scripts/eval.py:101-310 (also on trajectories logged with
+  different PD gains, at env batch sizes that split files across chunks)
 * compute_cost  scripts/mass_opt.py:62-76;  mass_sweep  scripts/mass_landscape.py:111-128
 * format_data  scripts/data/common.py:83-100
 * ActiveSysId.sample_commands / _sample_constant / _sample_polynomial /
@@ -46,7 +46,7 @@ from oracle import dynamics as dyn  # noqa: E402
 from oracle import go2_model as gm  # noqa: E402
 from oracle import sysid as osy  # noqa: E402
 
-REF = Path(os.environ.get("SPI_REFERENCE", "/root/reference"))
+REF = Path(os.environ["SPI_REFERENCE"]) if os.environ.get("SPI_REFERENCE") else None
 
 
 def extract(relpath, name, cls=None):
@@ -296,9 +296,7 @@ def ground_truth(rng, sim_params, n_traj=2, T=40):
                  else v) for k, v in f.items()} for f in frames]
 
 
-def evaluate_golden(rng):
-    sp = gm.SimParams(torque_speed=False)
-    trajs = ground_truth(rng, sp)
+def _eval_functions():
     ev_names = ["DatasetBatch", "MassEvalResult", "load_dataset", "to_device",
                 "capture_reference_masses", "apply_pd_gains_batch", "apply_base_mass",
                 "evaluate_batch"]
@@ -309,6 +307,13 @@ def evaluate_golden(rng):
               extra={"mass_eval": mass_eval, "Iterable": object})
     mo = load("scripts/mass_opt.py", ["compute_cost"],
               extra={"COST_COEFF": {"base_pos": 10.0, "base_quat": 5.0, "joint_pos": 1.0}})
+    return ev, ml, mo
+
+
+def evaluate_golden(rng):
+    sp = gm.SimParams(torque_speed=False)
+    trajs = ground_truth(rng, sp)
+    ev, ml, mo = _eval_functions()
     with tempfile.TemporaryDirectory() as td:
         paths = []
         for k, t in enumerate(trajs):
@@ -410,15 +415,64 @@ def commands_golden(rng):
         steps_per_update=25, poly_degree=3, bezier_points=4, n_updates=4, **out)
 
 
+# ----------------------------------------------------------------------------
+# 3b. evaluate_batch / mass_sweep on trajectories logged with different PD gains
+# ----------------------------------------------------------------------------
+MIXED_GAINS = ((20.0, 0.5), (25.0, 0.6), (17.0, 0.4))
+
+
+def evaluate_mixed_golden(rng):
+    """Three trajectories, each logged (and stored) with its own Kp / Kd; env batch sizes 16,
+    40 and 50 put windows of several files into one chunk, whose gains are its first row's."""
+    ev, ml, mo = _eval_functions()
+    trajs = []
+    for kp, kd in MIXED_GAINS:
+        sp_k = gm.SimParams(torque_speed=False, kp=np.full(12, kp), kd=np.full(12, kd))
+        trajs += ground_truth(rng, sp_k, n_traj=1)
+    sp = gm.SimParams(torque_speed=False)
+    H = 5
+    with tempfile.TemporaryDirectory() as td:
+        paths = []
+        for k, t in enumerate(trajs):
+            p = Path(td) / f"gt{k}.npz"
+            np.savez(p, **t)
+            paths.append(p)
+        n, ds_np = ev["load_dataset"](paths, H)
+    results = {}
+    for batch in (16, 40, 50):
+        env = make_fake_env(batch, sp)
+        ds = ev["to_device"](ds_np, torch.device("cpu"))
+        ref_masses = ev["capture_reference_masses"](env.simulator)
+        action_buffer = torch.zeros(batch, 12)
+        for s in (0.8, 1.0, 1.3):
+            ev["apply_base_mass"](env.simulator, ref_masses, float(ref_masses[0]) * float(s))
+            r = ev["evaluate_batch"](env, H, action_buffer, ds)
+            results[f"b{batch}_s{s}"] = np.array([r.base_pos, r.base_quat, r.joint_pos])
+    env = make_fake_env(40, sp)
+    ds = ev["to_device"](ds_np, torch.device("cpu"))
+    ref_masses = ev["capture_reference_masses"](env.simulator)
+    scales = np.linspace(0.5, 2.0, 20)
+    land = ml["mass_sweep"](env, ds, H, ref_masses, scales)
+    total = np.array([mo["compute_cost"](row) for row in land])
+    out = {f"traj{k}_{kk}": v for k, t in enumerate(trajs) for kk, v in t.items()
+           if kk != "robot_type"}
+    out.update({f"res_{k}": v for k, v in results.items()})
+    np.savez(HERE / "evaluate_mixed.npz", n_traj=len(trajs), horizon=H, sim_dt=sp.sim_dt,
+             decimation=sp.decimation, landscape_scales=scales, landscape=land,
+             landscape_total=total, landscape_argmin=int(np.argmin(total)), **out)
+
+
 def main():
-    if not REF.is_dir():
-        raise SystemExit(f"reference checkout not found at {REF}")
+    if REF is None or not REF.is_dir():
+        raise SystemExit("set SPI_REFERENCE to the path of a reference checkout "
+                         f"(got {os.environ.get('SPI_REFERENCE')!r})")
     rng = np.random.default_rng(20261203)
     motor_golden(rng)
     dataset_golden(rng)
     evaluate_golden(rng)
     fisher_golden(rng)
     commands_golden(rng)
+    evaluate_mixed_golden(rng)
     print("golden vectors written to", HERE)
 
 

@@ -81,6 +81,31 @@ def test_evaluate_batch_matches_reference(golden):
         np.testing.assert_allclose(res, g[key], rtol=1e-5, atol=1e-8, err_msg=key)
 
 
+def test_evaluate_batch_mixed_gains_matches_reference(golden):
+    """Trajectories logged with different Kp / Kd: each env-batch chunk runs with its first
+    row's gains (scripts/eval.py:243-250), at batch sizes that put several files in one chunk."""
+    g = golden("evaluate_mixed")
+    sim = gm.SimParams(torque_speed=False, sim_dt=float(g["sim_dt"]), decimation=int(g["decimation"]))
+    _, ds = ow.load_dataset(_trajs(g, int(g["n_traj"])), int(g["horizon"]))
+    assert len(np.unique(ds["pd_gain_kp"][:, 0])) == 3
+    for key in g.files:
+        if not key.startswith("res_"):
+            continue
+        batch, scale = key[4:].split("_")
+        th = gm.THETA_NOMINAL.copy()
+        th[0] = np.float32(gm.BASE_MASS) * np.float32(float(scale[1:]))
+        res = osy.evaluate_reference(ds, th, int(batch[1:]), sim)[0]
+        np.testing.assert_allclose(res, g[key], rtol=1e-5, atol=1e-8, err_msg=key)
+    # the same data scored with one gain set for every window gives different numbers
+    one = {k: (np.repeat(v[:1], len(v), 0) if k.startswith("pd_gain") else v) for k, v in ds.items()}
+    res_one = osy.evaluate_reference(one, gm.THETA_NOMINAL, 40, sim)[0]
+    assert np.max(np.abs(res_one - g["res_b40_s1.0"]) / np.abs(g["res_b40_s1.0"])) > 1e-3
+    scales = g["landscape_scales"].astype(np.float32).astype(np.float64)
+    costs, total, amin = osy.landscape(ds, scales, 40, sim)
+    np.testing.assert_allclose(costs, g["landscape"], rtol=1e-5, atol=1e-8)
+    assert amin == int(g["landscape_argmin"])
+
+
 def test_mass_landscape_argmin_matches_reference(golden):
     g = golden("evaluate")
     sim = gm.SimParams(torque_speed=False, sim_dt=float(g["sim_dt"]), decimation=int(g["decimation"]))

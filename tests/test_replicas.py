@@ -37,3 +37,20 @@ def test_whole_job_rate_over_two_gloo_ranks():
         assert rk == rank and world == 2
         assert ms == 200.0                              # the slower rank's time on every rank
         assert value == pytest.approx(2 * 1000.0 / 0.2)  # both ranks' units over that time
+
+
+def test_bench_gpus_2_relaunches_two_ranks():
+    """bench.py --gpus 2 started as a plain process runs two ranks itself and reports n_gpus 2
+    with the slowest rank's time (the launch check: the same plumbing, a host workload)."""
+    import json
+    import subprocess
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parent.parent
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, str(root / "bench.py"), "--gpus", "2", "--launch-check", "--steps", "3",
+                        "--warmup", "1"], capture_output=True, text=True, timeout=300, env=env, cwd=root)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1])
+    assert line["n_gpus"] == 2
+    assert line["value"] == pytest.approx(2 * 8.0 * 3 / (line["slowest_rank_ms"] * 1e-3))

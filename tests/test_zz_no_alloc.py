@@ -5,8 +5,10 @@ reserves its whole HBM budget at start-up, a host framework that owns every devi
 allocation, or a loop where cudaMalloc's implicit device synchronisation would stall other
 streams. These tests call it through the C ABI with caller-owned buffers and check it
 against the engine path (spi_load_windows + spi_set_theta + spi_run + spi_read_costs) on
-two calls in a row, with the same 1e-4 tolerance the other parity tests use. This file is
-collected last so that a failing run that stops at the first failure has run everything else.
+two calls in a row, with the same 1e-4 tolerance the other parity tests use; once with every
+optional argument left out (no weights, default squared-error weights, norm <= 0, no comp);
+and against the FP64 oracle's rollout and cost. This file is collected last so that a
+failing run that stops at the first failure has run everything else.
 """
 import ctypes
 
@@ -98,3 +100,54 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
                                       comp.data_ptr(), None, None)
     assert rc == -1
     assert b"exceeds the fixed scratch" in lib.spi_last_error()
+
+
+def test_noalloc_optional_arguments_left_out():
+    """weight NULL (all 1), sq_weights NULL (built-in defaults), norm 0 (divide by W), comp NULL."""
+    from spi_gb300 import _lib, robot as rb
+    from spi_gb300.engine import COST_SQ, Engine
+    lib = _lib.engine_lib()
+    cfg = rb.SimConfig()
+    robot = rb.to_struct(cfg)
+    W, H, N = 21, 4, 19
+    host = _windows(8, W, H)
+    dev_in = [torch.from_numpy(a).cuda() for a in host[:3]]
+    eng = Engine(cfg)
+    eng.load_windows(dev_in[0], dev_in[1], dev_in[2], None, norm=None)
+    eng.set_cost(COST_SQ)
+    theta = torch.from_numpy(_theta(9, N)).cuda()
+    _, ref_cost = eng.evaluate(theta)
+    cost = torch.full((N,), float("nan"), device="cuda")
+    rc = lib.spi_eval_windows_noalloc(ctypes.byref(robot), dev_in[0].data_ptr(), dev_in[1].data_ptr(),
+                                      dev_in[2].data_ptr(), None, W, H, 0.0, theta.data_ptr(), N, 1, None,
+                                      None, cost.data_ptr(), None)
+    assert rc == 0, lib.spi_last_error()
+    torch.cuda.synchronize()
+    assert torch.isfinite(cost).all()
+    assert _rel_err(cost.cpu(), ref_cost.cpu()) <= TOL
+
+
+def test_noalloc_matches_fp64_oracle():
+    """Rollout and weighted cost against the FP64 oracle on the same windows and theta."""
+    from oracle import cost as oc
+    from oracle import dynamics as dyn
+    from oracle import go2_model as gm
+    from spi_gb300 import _lib, robot as rb
+    lib = _lib.engine_lib()
+    robot = rb.to_struct(rb.SimConfig())
+    W, H, N = 13, 5, 6
+    init, actions, target, weight = _windows(11, W, H)
+    norm = float(weight.sum())
+    dev_in = [torch.from_numpy(a).cuda() for a in (init, actions, target, weight)]
+    theta = torch.from_numpy(_theta(12, N)).cuda()
+    for mode in (1, 0):
+        comp, cost = _noalloc(lib, robot, dev_in, theta, W, H, norm, mode)
+        torch.cuda.synchronize()
+        th = theta.cpu().numpy().astype(np.float64)
+        fin = dyn.rollout(np.tile(init.astype(np.float64), (N, 1)), np.tile(actions.astype(np.float64), (N, 1, 1)),
+                          np.repeat(th, W, 0), gm.SimParams())
+        wc = oc.window_components(fin, np.tile(target.astype(np.float64), (N, 1))).reshape(N, W, oc.N_COMP)
+        ref_comp = oc.reduce_components(wc, weight, norm)
+        ref_cost = oc.scalar_cost(ref_comp, mode="sq" if mode == 1 else "ref")
+        assert _rel_err(comp.cpu(), ref_comp) <= TOL, mode
+        assert _rel_err(cost.cpu(), ref_cost) <= TOL, mode
