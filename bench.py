@@ -358,32 +358,39 @@ def recorded_dram_bytes(kernel: str):
 
 def identification_report(cem, eng, theta_true):
     """Per-parameter result of the CEM identification, and which parameters the excitation
-    leaves unidentified. The information check: F = sum_w J_w^T Q J_w at the true theta over
-    the loaded windows (forward-mode sensitivities, Q the cost's state weights); for each
-    parameter sqrt((F^-1)_ii) / (hi - lo) is the cost-curvature std in units of its prior range,
-    so a large value means the windows barely constrain that parameter."""
+    cannot identify. The information check: F = mean_w J_w^T Q J_w at the true theta over the
+    loaded windows (forward-mode sensitivities, Q the cost's state weights), so that the cost
+    near the truth is about d^T F d for a parameter offset d. With the other parameters refit,
+    moving parameter i by r raises the cost by r^2 / (F^-1)_ii; resolution_frac is the offset
+    (in units of its prior range) at which that rise equals the best cost reached, i.e. the
+    smallest error the windows can tell apart from the achieved fit."""
     import torch
     from spi_gb300.engine import DEFAULT_SQ_WEIGHTS
     from spi_gb300.robot import THETA_NAMES
     from spi_gb300.sensitivity import block_weights, sensitivities
     te = cem.theta_errors(theta_true)
+    best = cem.best_cost()
     J, _ = sensitivities(eng, np.asarray(theta_true, np.float32)[None], cem.param_ids)
     q = torch.as_tensor(block_weights(DEFAULT_SQ_WEIGHTS), device=J.device, dtype=torch.float64)
     Jd = J[0].double()                                             # [W, 37, K]
     F = torch.einsum("wik,i,wil->kl", Jd, q, Jd).cpu().numpy() / J.shape[1]
     rng = cem.hi - cem.lo
     Fs = F * np.outer(rng, rng)                                    # in prior-range units
-    crlb = np.sqrt(np.maximum(np.diag(np.linalg.pinv(Fs + 1e-12 * np.trace(Fs) * np.eye(len(rng)))), 0.0))
+    Finv = np.linalg.pinv(Fs + 1e-12 * np.trace(Fs) * np.eye(len(rng)))
+    resolution = np.sqrt(np.maximum(best, 0.0) * np.maximum(np.diag(Finv), 0.0))
     names = [THETA_NAMES[i] for i in cem.param_ids]
     per = {n: {"true": float(t), "est": float(e), "err_frac": float(ef), "std_frac": float(sf),
-               "info_std_frac": float(c)}
-           for n, t, e, ef, sf, c in zip(names, te["true"], te["est"], te["err_frac"], te["std_frac"], crlb)}
+               "resolution_frac": float(r)}
+           for n, t, e, ef, sf, r in zip(names, te["true"], te["est"], te["err_frac"], te["std_frac"], resolution)}
     worst = int(np.argmax(te["err_frac"]))
-    return {"best_cost": cem.best_cost(), "theta_err": float(te["err_frac"][worst]), "theta_err_param": names[worst],
+    return {"best_cost": best, "theta_err": float(te["err_frac"][worst]), "theta_err_param": names[worst],
             "per_param": per,
             "not_identified": [n for n, ef in zip(names, te["err_frac"]) if ef > 0.1],
-            "note": "err_frac = |CEM mean - truth| / prior range; info_std_frac = sqrt((F^-1)_ii) / prior range "
-                    "from the exact Fisher information of the cost at the truth over the 256 windows"}
+            "unidentifiable": [n for n, r in zip(names, resolution) if r > 0.1],
+            "note": "err_frac = |CEM mean - truth| / prior range; resolution_frac = sqrt(best_cost (F^-1)_ii) / "
+                    "prior range from the exact Fisher information at the truth over the loaded windows: above "
+                    "0.1 the windows carry too little information on that parameter (e.g. torque-limit scales "
+                    "when no motor reaches its limit)"}
 
 
 def run_rollout_case(args):

@@ -210,6 +210,38 @@ int spi_fisher(const float* J, int N, int W, int K, const float* state_weight, d
 int spi_fisher_ex(const float* J, int N, int W, int K, const float* state_weight, double eps, int tensor_cores,
                   float* F, double* logdet, double* trace, void* stream);
 
+/* ---- the device CEM over a caller-scored population ----------------------------------------
+ * Replaces the Optuna ask / tell of the reference's excitation search
+ * (spigym/agents/sysid/active_sysid.py:165-257; CmaEsSampler, spigym/config/algo/
+ * active_sysid.yaml:20) for searches whose candidates are not scored by spi_run. The same
+ * sampling and refit kernels as spi_cem_*: spi_search_sample draws a population [n][13] into a
+ * buffer the search owns (the identified slots sampled, the others at cfg->nominal) and returns
+ * its device address; spi_search_refit takes the caller's device costs [n] (lower is better).
+ * All calls are asynchronous on `stream` except create and read. */
+typedef struct spi_search spi_search;
+int spi_search_create(const spi_cem_config* cfg, void* stream, spi_search** out);
+int spi_search_destroy(spi_search* s);
+int spi_search_sample(spi_search* s, float** population);
+int spi_search_refit(spi_search* s, const float* cost);
+/* Synchronous: mean [P], covariance [P][P], best candidate [13] and cost, iterations done. */
+int spi_search_read(spi_search* s, double* mu, double* cov, float* best, float* best_cost, int32_t* iteration);
+
+/* ---- the reference's finite-difference Fisher objective -------------------------------------
+ * spi_fd_fisher runs the open-loop active-sysid episode of the reference for C candidate
+ * excitations at once: spigym/envs/sysid/active_sysid_openloop.py:29-80 (each candidate is a
+ * group of 1 main + P aux rollouts, aux k at theta + delta on slot param_ids[k]), :246-252 and
+ * :316-330 (after 1-based control step t with t % ksync == 1, or after every step when
+ * ksync <= 1, the aux rollouts take the main's state) and :402-426 (after every step the reward
+ * trace(J^T J), J = (s_main - s_aux) / delta over the 13 root-state entries and 12 joint
+ * positions). x0 device [C][37] start states, actions device [C][T][12], theta device [C][13]
+ * (each group's main theta), param_ids host [P] (P <= 13, distinct slots). reward_sum device
+ * [C] receives the reward summed over steps t > skip (1-based); reward_trace device [C][T] each
+ * step's reward, or NULL. Asynchronous on the engine stream; the engine's windows and theta
+ * batch are not used. */
+int spi_fd_fisher(spi_engine* e, const float* x0, const float* actions, const float* theta, int C, int T,
+                  const int32_t* param_ids, int P, float delta, int ksync, int skip, float* reward_sum,
+                  float* reward_trace);
+
 /* ---- continuous-batching identification server ------------------------------------------
  * Many sysid jobs of uneven population, window count, horizon and parameter dimension share
  * the GPU. Each job is one CEM identification (the work of scripts/mass_opt.py per dataset);

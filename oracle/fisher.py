@@ -38,3 +38,60 @@ def fisher_logdet(F, eps=1e-6):
     P = F.shape[-1]
     L = np.linalg.cholesky(F + eps * np.eye(P))
     return 2.0 * np.sum(np.log(np.diagonal(L, axis1=-2, axis2=-1)), -1)
+
+
+def fd_fisher_episode(x0, actions, theta, param_ids, delta, ksync, sim, reset_step=True):
+    """The reference's open-loop active-sysid episode for C candidates, step by step.
+
+    Restates, in FP64 on the oracle's dynamics:
+    * the env layout of active_sysid_openloop.py:51-80: every candidate is a group of 1 main
+      + P aux envs, aux k with +delta on parameter param_ids[k];
+    * reset_all (:116-131 over base_task.reset_all) running one zero-action step, with
+      step_idx = 1 after it, before the policy loop (reset_step);
+    * per step (_pre_physics_step :170-172 increments step_idx; _post_physics_step
+      :209-252): the reward ``fd_fisher_reward`` of the new states, then, when
+      step_idx % ksync == 1 (every step if ksync <= 1), the aux states set to the main's
+      (_reset_envs_states_to_main_envs :316-330);
+    * evaluate_policy (active_sysid.py:527-600): rewards of the loop steps summed and divided
+      by the loop's step counter, which ends one above the number of steps.
+
+    x0 [C, 37], actions [C, n, 12], theta [C, 13]. Returns (mean reward [C], per-step rewards
+    [C, n] of the loop steps)."""
+    from . import dynamics as dyn
+    x0 = np.asarray(x0, dtype=np.float64)
+    actions = np.asarray(actions, dtype=np.float64)
+    C, n = actions.shape[:2]
+    theta = np.broadcast_to(np.atleast_2d(np.asarray(theta, dtype=np.float64)), (C, 13))
+    P = len(param_ids)
+    G = P + 1
+    th = np.repeat(theta, G, 0)
+    for k, s in enumerate(param_ids):
+        th[k + 1::G, s] += delta
+    x = np.repeat(x0, G, 0)
+    main = np.arange(C) * G
+    origins = np.zeros((C * G, 3))
+
+    def reward(xs):
+        return fd_fisher_reward(xs[:, :13], xs[:, 13:25], origins, C, P, delta)[main]
+
+    def resync(xs, step_idx):
+        if ksync <= 1 or step_idx % ksync == 1:
+            xs = xs.copy()
+            for k in range(1, G):
+                xs[main + k] = xs[main]
+        return xs
+
+    step_idx = 0
+    if reset_step:
+        x = dyn.control_step(x, np.zeros((C * G, 12)), th, sim)
+        step_idx = 1
+        x = resync(x, step_idx)
+    per_step = np.zeros((C, n))
+    step = 1
+    for t in range(n):
+        x = dyn.control_step(x, np.repeat(actions[:, t], G, 0), th, sim)
+        step_idx += 1
+        per_step[:, t] = reward(x)
+        x = resync(x, step_idx)
+        step += 1
+    return per_step.sum(1) / step, per_step

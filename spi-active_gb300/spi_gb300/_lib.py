@@ -49,6 +49,13 @@ ENGINE_API = {
     "spi_fisher_ex": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_double, c_int, c_void_p, c_void_p,
                               c_void_p, c_void_p]),
     "spi_probe_fp32_peak": (c_int, [POINTER(c_double)]),
+    "spi_search_create": (c_int, [c_void_p, c_void_p, POINTER(c_void_p)]),
+    "spi_search_destroy": (c_int, [c_void_p]),
+    "spi_search_sample": (c_int, [c_void_p, POINTER(c_void_p)]),
+    "spi_search_refit": (c_int, [c_void_p, c_void_p]),
+    "spi_search_read": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "spi_fd_fisher": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, POINTER(ctypes.c_int32), c_int,
+                              c_float, c_int, c_int, c_void_p, c_void_p]),
     "spi_eval_windows_noalloc": (c_int, [POINTER(SpiRobot), c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int,
                                          c_float, c_void_p, c_int, c_int, POINTER(c_float), c_void_p, c_void_p,
                                          c_void_p]),
