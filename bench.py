@@ -320,6 +320,7 @@ def run_c3(args):
                    "tensor_tflops": f_flops / f_s / 1e12, "tensor_frac": f_flops / f_s / 1e12 / bf16_peak,
                    "note": "13 x 13 Gram matrices over 296 rows per candidate: too small for either roof "
                            "(one warp per candidate, latency-bound); peaks from MEASURED_PEAKS.json"}
+    grad_line = gradient_throughput(eng, args)
     tangent_steps = n * wpc * H * 13
     primal_steps = n * (settle + wpc * H)
     line = {"metric": "excitation candidates scored/s", "value": n / t, "unit": "candidates/s", "n_gpus": 1,
@@ -333,6 +334,7 @@ def run_c3(args):
             "rollout_steps_per_s": (tangent_steps + primal_steps) / t,
             "tangent_rollout_steps_per_step": tangent_steps, "primal_rollout_steps_per_step": primal_steps,
             "fisher_ms": fisher_ms, "fisher_roofline": fisher_roof, "best_candidate": int(r["best"]),
+            "gradient": grad_line,
             "logdet_range": [float(np.min(r["logdet"])), float(np.max(r["logdet"]))],
             "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
@@ -434,6 +436,45 @@ def run_rollout_case(args):
                                              f"H={args.horizon}, one spi_run launch timed",
                                  "kernel_variant": args.variant},
                       "median_cost": float(cost.median())}), flush=True)
+
+
+def gradient_throughput(eng, args, n_theta=512, n_windows=256, horizon=20):
+    """d cost / d theta of the squared-error window cost for n_theta prior samples against
+    n_windows windows x H = 20 (13 parameters): one hand-written adjoint sweep per rollout
+    (spi_adjoint, checkpoints every 5 control steps) against 13 forward-mode tangent sweeps
+    (spi_sensitivity). CUDA-event times on the engine stream after a warm-up call of each."""
+    import torch
+    from spi_gb300 import robot
+    from spi_gb300.data import synthetic_windows
+    from spi_gb300.engine import COST_SQ
+    from spi_gb300.sensitivity import adjoint, tangent_gradient
+    rng = np.random.default_rng(12)
+    lo, hi = robot.THETA_PRIOR_LO, robot.THETA_PRIOR_HI
+    init, act, tgt = synthetic_windows(eng, lo + (hi - lo) * rng.random(13), n_windows, horizon, seed=21)
+    eng.load_windows(torch.from_numpy(init), torch.from_numpy(act), torch.from_numpy(tgt))
+    eng.set_cost(COST_SQ)
+    th = torch.from_numpy((lo + (hi - lo) * rng.random((n_theta, 13))).astype(np.float32)).cuda()
+    out = {}
+    for name, fn in (("adjoint", lambda: adjoint(eng, th)), ("tangent_13", lambda: tangent_gradient(eng, th))):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = max(1, min(args.steps, 5))
+        e0.record(eng.stream)
+        for _ in range(reps):
+            res = fn()
+        e1.record(eng.stream)
+        e1.synchronize()
+        out[name] = (e0.elapsed_time(e1) / reps, res)
+    (ta, (ca, ga)), (tt, (ct, gt)) = out["adjoint"], out["tangent_13"]
+    ga, gt = ga.double(), gt.double()
+    rel = float(((ga - gt).norm(dim=1) / gt.norm(dim=1).clamp(min=1e-30)).max())
+    rollouts = n_theta * n_windows
+    return {"workload": f"{n_theta} theta x {n_windows} windows x H={horizon}, 13 parameters, squared-error cost",
+            "adjoint_ms": ta, "tangent_13_ms": tt, "speedup_adjoint_over_tangent": tt / ta,
+            "adjoint_rollout_gradients_per_s": rollouts / (ta * 1e-3),
+            "tangent_rollout_gradients_per_s": rollouts / (tt * 1e-3),
+            "max_rel_diff_adjoint_vs_tangent": rel, "nonfinite_rollouts": eng.sync()}
 
 
 def run_reference(args):

@@ -210,6 +210,18 @@ int spi_fisher(const float* J, int N, int W, int K, const float* state_weight, d
 int spi_fisher_ex(const float* J, int N, int W, int K, const float* state_weight, double eps, int tensor_cores,
                   float* F, double* logdet, double* trace, void* stream);
 
+/* ---- gradient by the adjoint of the rollout ------------------------------------------------
+ * The reference has no gradient: its active exploration differences a main env against aux envs
+ * with theta + 0.1 (spigym/envs/sysid/active_sysid_openloop.py:402-426). spi_adjoint gives, for
+ * theta device [N][13] against the loaded windows, cost[n] = the engine's cost (spi_set_cost
+ * mode and weights, the window weights and normaliser of spi_load_windows) and grad[n][13] =
+ * d cost[n] / d theta[n] by a hand-written reverse sweep of the rollout: the forward pass keeps
+ * the state every 5 control steps, the reverse pass recomputes each 5-step segment forward and
+ * runs the substep adjoints backwards through it. cost and grad are device pointers (either may
+ * be NULL). Non-finite final states are counted as by spi_run (spi_sync). Asynchronous on the
+ * engine stream. */
+int spi_adjoint(spi_engine* e, const float* theta, int N, float* cost, float* grad);
+
 /* ---- the device CEM over a caller-scored population ----------------------------------------
  * Replaces the Optuna ask / tell of the reference's excitation search
  * (spigym/agents/sysid/active_sysid.py:165-257; CmaEsSampler, spigym/config/algo/

@@ -538,6 +538,14 @@ template <class T> struct LegWork {
   }
 };
 
+// Work records that also want the inverse pivots of M = L D L^T (D^-1 = diag(i0, i1, i2)) define
+// put_diag; phase A hands them over only to those (overload resolution on the int / long tag).
+template <class WK, class T>
+SPI_INL auto put_diag_if(WK& w, T i0, T i1, T i2, int) -> decltype(w.put_diag(i0, i1, i2), void()) {
+  w.put_diag(i0, i1, i2);
+}
+template <class WK, class T> SPI_INL void put_diag_if(WK&, T, T, T, long) {}
+
 template <class T> SPI_INL M3<T> quat_to_R(T x, T y, T z, T w) {
   M3<T> R;
   R.m[0][0] = T(1) - T(2) * (y * y + z * z); R.m[0][1] = T(2) * (x * y - z * w); R.m[0][2] = T(2) * (x * z + y * w);
@@ -880,6 +888,7 @@ SPI_INL void phase_a_core(const DevModel& M, int leg, const BaseState<T>& B, con
   const T e12 = M12 - l20 * M01;
   const T l21 = e12 * i1;
   const T i2 = T(1) / (M22 - l20 * M02 - l21 * e12);
+  put_diag_if(W, i0, i1, i2, 0);
   // K = F L^-T (base coordinates), K' = K D^-1, y = D^-1 L^-1 (tau - C)
   // (F0h.v.x = 0 and F1h.v.y = F2h.v.y = 0 by construction, so K0.v.x = 0)
   const SV<T> K0 = hip_col_to_base_vx0(F0h, C[0], S[0], r0);

@@ -31,6 +31,7 @@ struct spi_engine {
   cudaStream_t capture_stream = nullptr;   // graphs are captured here, replayed on `stream`
   unsigned seen_generation = 0;            // buffer generations the graph / CEM pointers refer to
   spi::DeviceBuf sens_ids;                 // sensitivity directions (theta slots)
+  spi::DeviceBuf adj_ckpt, adj_seg, adj_part;   // adjoint checkpoints, segment states, partials
   int h_sens_ids[SPI_THETA_DIM] = {0};
 };
 

@@ -49,6 +49,7 @@ ENGINE_API = {
     "spi_fisher_ex": (c_int, [c_void_p, c_int, c_int, c_int, c_void_p, c_double, c_int, c_void_p, c_void_p,
                               c_void_p, c_void_p]),
     "spi_probe_fp32_peak": (c_int, [POINTER(c_double)]),
+    "spi_adjoint": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_void_p]),
     "spi_search_create": (c_int, [c_void_p, c_void_p, POINTER(c_void_p)]),
     "spi_search_destroy": (c_int, [c_void_p]),
     "spi_search_sample": (c_int, [c_void_p, POINTER(c_void_p)]),
@@ -102,5 +103,10 @@ def hostemu_lib():
                                               POINTER(ctypes.c_longlong), POINTER(ctypes.c_longlong)]
         lib.spi_hostemu_count_ops_aba.restype = c_int
         lib.spi_hostemu_count_ops_aba.argtypes = lib.spi_hostemu_count_ops.argtypes
+        lib.spi_hostemu_grad.restype = c_int
+        lib.spi_hostemu_grad.argtypes = [POINTER(SpiRobot), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
+                                         c_int, c_int, c_void_p, c_void_p]
+        lib.spi_hostemu_residual.restype = c_int
+        lib.spi_hostemu_residual.argtypes = [POINTER(SpiRobot), c_void_p, c_void_p, c_void_p, c_void_p]
         _hostemu = lib
     return _hostemu

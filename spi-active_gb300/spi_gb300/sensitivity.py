@@ -1,5 +1,8 @@
 """State sensitivities, Fisher information and excitation scoring (spi_sensitivity / spi_fisher).
 
+Gradients of the windowed cost in theta come from the hand-written adjoint of the rollout
+(``adjoint``, ``WindowCost``); per-window Jacobians from forward-mode derivatives.
+
 The reference scores candidate excitations with a finite-difference Fisher proxy:
 main and auxiliary envs with theta + 0.1 (spigym/envs/sysid/active_sysid_openloop.py:29-80,
 402-426) and trace(J^T J) as the objective. Here J_w = d s_H / d theta comes from forward-mode
@@ -55,26 +58,53 @@ def block_weights(sq_weights):
     return np.concatenate([np.full(n, w, np.float32) for n, w in zip(sizes, sq_weights)])
 
 
-class WindowCost(torch.autograd.Function):
-    """Weighted squared final-state error per theta sample, differentiable in theta.
+def adjoint(engine, theta):
+    """(cost [N], d cost / d theta [N, 13]) of the engine's cost by the hand-written adjoint
+    (spi_adjoint): one reverse sweep per rollout, checkpoints every 5 control steps."""
+    theta = torch.as_tensor(theta, dtype=torch.float32, device=engine.device).reshape(-1, THETA_DIM).contiguous()
+    N = theta.shape[0]
+    cost = torch.empty((N,), device=engine.device)
+    grad = torch.empty((N, THETA_DIM), device=engine.device)
+    with torch.cuda.device(engine.device):
+        _lib.check(engine.lib.spi_adjoint(engine._h, theta.data_ptr(), N, cost.data_ptr(), grad.data_ptr()))
+    engine._adj_keep = theta
+    return cost, grad
 
-    forward(theta [N,13], engine, sq_weights) -> cost [N] = mean_w sum_i q_i (s_H,i - target_i)^2
-    over the engine's windows; the gradient comes from the forward-mode sensitivities.
+
+def tangent_gradient(engine, theta, sq_weights=(10.0, 5.0, 0.1, 0.1, 1.0, 0.01)):
+    """The same gradient of the squared-error cost from the 13 forward-mode tangent sweeps
+    (d cost / d theta = 2 sum_w diff_w^T Q J_w / W), for comparison with ``adjoint``."""
+    J, xH = sensitivities(engine, theta, list(range(THETA_DIM)))
+    q = torch.as_tensor(block_weights(sq_weights), device=J.device)
+    diff = xH - engine.target[None]
+    cost = (q * diff * diff).sum(-1).mean(1)
+    return cost, 2.0 * torch.einsum("nwi,i,nwik->nk", diff, q, J) / engine.W
+
+
+class WindowCost(torch.autograd.Function):
+    """The engine's squared-error cost per theta sample, differentiable in theta.
+
+    forward(theta [N,13], engine, sq_weights) -> cost [N] = sum_w weight_w sum_i q_i
+    (s_H,i - target_i)^2 / norm over the engine's windows (mean over windows for unit weights),
+    from one spi_run; backward runs the hand-written adjoint of the rollout (``adjoint``) for
+    d cost / d theta. The per-window Jacobians d s_H / d theta stay with the forward-mode
+    ``sensitivities`` (13 directions against 37 outputs).
     """
 
     @staticmethod
     def forward(ctx, theta, engine, sq_weights):
-        J, xH = sensitivities(engine, theta.detach(), list(range(THETA_DIM)))
-        q = torch.as_tensor(block_weights(sq_weights), device=theta.device)
-        diff = xH - engine.target[None]
-        cost = (q * diff * diff).sum(-1).mean(1)
-        grad = 2.0 * torch.einsum("nwi,i,nwik->nk", diff, q, J) / engine.W
-        ctx.save_for_backward(grad)
-        return cost
+        from .engine import COST_SQ
+        engine.set_cost(COST_SQ, sq_weights)
+        th = theta.detach().to(torch.float32).contiguous()
+        _, cost = engine.evaluate(th)
+        ctx.engine = engine
+        ctx.save_for_backward(th)
+        return cost.clone()
 
     @staticmethod
     def backward(ctx, g):
-        (grad,) = ctx.saved_tensors
+        (th,) = ctx.saved_tensors
+        _, grad = adjoint(ctx.engine, th)
         return g[:, None] * grad, None, None
 
 
