@@ -56,8 +56,8 @@ def parse_args():
     ap.add_argument("--runs", type=int, default=3, help="rollout-case: launches, the last one timed")
     ap.add_argument("--c3-candidates", type=int, default=512, help="c3: candidate excitations scored per step")
     ap.add_argument("--no-serving", action="store_true", help="c1: skip the served-vs-plain job mix")
-    ap.add_argument("--mix-jobs", type=int, default=16, help="c1: jobs in the served-vs-plain mix")
-    ap.add_argument("--mix-iters", type=int, default=10, help="c1: CEM iterations per job in the mix")
+    ap.add_argument("--mix-jobs", type=int, default=64, help="c1: jobs in each served-vs-plain mix")
+    ap.add_argument("--mix-iters", type=int, default=30, help="c1: CEM iterations per job in the mixes")
     ap.add_argument("--c2-jobs", type=int, default=64)
     ap.add_argument("--c4-rate", type=float, default=200.0, help="c4: arrivals per second")
     ap.add_argument("--c4-jobs", type=int, default=64, help="c4: jobs in the stream")
@@ -238,6 +238,46 @@ def served_vs_plain(specs, realtime, cfg=None, variant="lane4"):
                                                 "max": float(ratios.max())}
     out["jobs"] = len(specs)
     out["kernel_variant"] = variant
+    return out
+
+
+def serving_mixes(args, variant, ceiling):
+    """Served (continuous batching) against plain (one job at a time) on the job mixes the
+    throughput / latency half of the metric is stated on, each with its served rate as a
+    fraction of the single-job kernel ceiling (`ceiling`: the c1 rollout-steps/s of this run):
+    * c2: 64 jobs, population U{256..4096}, windows U{16..512}, horizon U{5..50}, parameters
+      U{1..13}, 30 CEM iterations each, all submitted at t = 0;
+    * c4: the same size distribution as a Poisson stream at 200 jobs/s with 20 % of the jobs also
+      asking for an excitation score, bounded to 64 arrivals (about 0.3 s of arrivals; the full
+      60 s stream offers ~100x what one GPU serves and would run for hours);
+    * small_jobs: 64 jobs of population U{64..512}, windows U{8..64}, horizon U{5..20}: each
+      alone leaves most SMs idle, the regime where batching raises throughput."""
+    from spi_gb300.server import Server
+    from spi_gb300.workloads import c2_specs, poisson_arrivals, small_specs
+    sv = variant if variant in Server.VARIANTS else "lane4"
+    n, it = args.mix_jobs, args.mix_iters
+    out = {}
+    mixes = (
+        ("c2", c2_specs(n, seed=2, iterations=it), False,
+         f"c2: {n} jobs (pop U{{256..4096}}, W U{{16..512}}, H U{{5..50}}, P U{{1..13}}), {it} CEM iterations "
+         "each, all submitted at t=0"),
+        ("c4", poisson_arrivals(c2_specs(n, seed=4, iterations=it), args.c4_rate, seed=4, fisher_frac=0.2), True,
+         f"c4: Poisson stream at {args.c4_rate:g} jobs/s of the c2 size distribution, {n} arrivals, {it} CEM "
+         "iterations each, 20% also score 32 candidate excitations, 150 GB HBM admission budget"),
+        ("small_jobs", small_specs(n, seed=3, iterations=it), False,
+         f"{n} small jobs (pop U{{64..512}}, W U{{8..64}}, H U{{5..20}}, P U{{1..13}}), {it} CEM iterations each, "
+         "all submitted at t=0"),
+    )
+    for name, specs, realtime, desc in mixes:
+        r = served_vs_plain(specs, realtime, variant=sv)
+        r["workload"] = desc
+        r["served_fraction_of_kernel_ceiling"] = r["served"]["rollout_steps_per_s"] / ceiling
+        r["plain_fraction_of_kernel_ceiling"] = r["plain"]["rollout_steps_per_s"] / ceiling
+        out[name] = r
+    out["kernel_ceiling_rollout_steps_per_s"] = ceiling
+    out["note"] = ("the plain engine already puts every (theta, window) pair of a job in one launch, so a job of "
+                   "the c2 sizes alone fills the GPU and the served rate is bounded by the same kernel ceiling: "
+                   "served / plain cannot approach 5x there; it rises where jobs are small")
     return out
 
 
@@ -644,17 +684,7 @@ def run_ours(args):
             "wall_s": wall, "nonfinite_rollouts": n_bad, "clocks": clocks.summary(),
             "cem": identification_report(cem, eng, theta_true)}
     if ws == 1 and not args.no_serving:
-        from spi_gb300.workloads import c2_specs, small_specs
-        from spi_gb300.server import Server
-        sv = variant if variant in Server.VARIANTS else "lane4"
-        mix = served_vs_plain(c2_specs(args.mix_jobs, seed=2, iterations=args.mix_iters), False, variant=sv)
-        mix["workload"] = (f"{args.mix_jobs} jobs of the c2 size distribution, {args.mix_iters} CEM iterations "
-                           "each, all submitted at t=0")
-        small = served_vs_plain(small_specs(4 * args.mix_jobs, seed=3, iterations=args.mix_iters), False,
-                                variant=sv)
-        small["workload"] = (f"{4 * args.mix_jobs} small jobs (pop U{{64..512}}, W U{{8..64}}, H U{{5..20}}), "
-                             f"{args.mix_iters} CEM iterations each, all submitted at t=0")
-        line["served_vs_plain"] = {"c2_mix": mix, "small_jobs": small}
+        line["served_vs_plain"] = serving_mixes(args, variant, value)
     if ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_seconds, H)
     print(json.dumps(line), flush=True)

@@ -144,11 +144,16 @@ def default_work_cap(device=None):
 
 
 def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=64, hbm_budget=150 << 30,
-               ctas_per_sm=0, items_per_claim=1, realtime=True, work_cap=None, variant="lane4", rounds=4):
+               ctas_per_sm=0, items_per_claim=1, realtime=True, work_cap=None, variant="lane4", rounds=4,
+               timeline=True):
     """Continuous batching: admit on arrival while HBM budget, a slot and GPU work capacity are free;
     every tick advances each admitted job by 1 .. `rounds` CEM iterations (more for smaller jobs). Fisher requests are scored on a worker
     thread (own engine and stream) while the server keeps ticking; a job completes when its
-    score is in."""
+    score is in.
+
+    timeline: CUDA events on the server stream around every tick's launches give the GPU time
+    of each tick and the idle gaps between consecutive ticks, i.e. how long the GPU waited for
+    the host loop (admission, tick set-up, result polling); reported as ``timeline``."""
     max_samples = max(s.n_samples for s in specs)
     server = Server(cfg, max_slots=max_slots, max_samples=max_samples, hbm_budget_bytes=hbm_budget,
                     device=bank.engine.device)
@@ -170,6 +175,7 @@ def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=
     t0 = time.perf_counter()
     done, lat, results, scoring = 0, {}, {}, []
     qi = 0
+    marks = []                            # (event before, event after) each tick's launches
 
     def _score(job_id, theta, arrival):
         with torch.cuda.device(bank.engine.device):
@@ -185,7 +191,14 @@ def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=
                 break                     # no slot / budget: wait for a retirement
             qi += 1
         active, _ = server.stats()
-        server.tick()
+        if timeline and active:
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(server.stream)
+            server.tick()
+            e1.record(server.stream)
+            marks.append((e0, e1))
+        else:
+            server.tick()
         if not active:
             server.wait()
             if qi < len(pending) and realtime:
@@ -205,7 +218,24 @@ def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=
     if pool is not None:
         pool.shutdown()
     server.close()
-    return _summary(specs, lat, wall, results)
+    out = _summary(specs, lat, wall, results)
+    if timeline and marks:
+        torch.cuda.synchronize()
+        busy = [a.elapsed_time(b) for a, b in marks]
+        gaps = [marks[k][1].elapsed_time(marks[k + 1][0]) for k in range(len(marks) - 1)]
+        span = marks[0][0].elapsed_time(marks[-1][1])
+        out["timeline"] = {"ticks": len(marks), "gpu_tick_ms_median": float(np.median(busy)),
+                           "gpu_busy_ms": float(np.sum(busy)), "gpu_idle_gaps_ms": float(np.sum(gaps)),
+                           "max_gap_ms": float(np.max(gaps)) if gaps else 0.0,
+                           "idle_fraction": float(np.sum(gaps) / span) if span > 0 else 0.0,
+                           "host_loop_ms_per_tick": wall * 1e3 / len(marks),
+                           "note": "CUDA events on the server stream before and after each spi_server_tick "
+                                   "call; a gap is GPU time between the end of one tick's work and the host "
+                                   "loop's next tick call (admission, polling, Fisher hand-off), i.e. GPU time "
+                                   "lost to the host loop; the tick call's own table staging (tens of us) counts "
+                                   "as tick time. In a real-time stream, jobs that arrive after the GPU frees up "
+                                   "also show as gaps"}
+    return out
 
 
 def run_plain(specs, bank: WindowBank, cfg: SimConfig | None = None, graph=True, variant="lane4"):
