@@ -360,6 +360,7 @@ def run_c3(args):
                    "tensor_tflops": f_flops / f_s / 1e12, "tensor_frac": f_flops / f_s / 1e12 / bf16_peak,
                    "note": "13 x 13 Gram matrices over 296 rows per candidate: too small for either roof "
                            "(one warp per candidate, latency-bound); peaks from MEASURED_PEAKS.json"}
+    fd_line = fd_fisher_throughput(eng, acts, args)
     grad_line = gradient_throughput(eng, args)
     tangent_steps = n * wpc * H * 13
     primal_steps = n * (settle + wpc * H)
@@ -374,7 +375,7 @@ def run_c3(args):
             "rollout_steps_per_s": (tangent_steps + primal_steps) / t,
             "tangent_rollout_steps_per_step": tangent_steps, "primal_rollout_steps_per_step": primal_steps,
             "fisher_ms": fisher_ms, "fisher_roofline": fisher_roof, "best_candidate": int(r["best"]),
-            "gradient": grad_line,
+            "gradient": grad_line, "fd_fisher": fd_line,
             "logdet_range": [float(np.min(r["logdet"])), float(np.max(r["logdet"]))],
             "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
@@ -476,6 +477,37 @@ def run_rollout_case(args):
                                              f"H={args.horizon}, one spi_run launch timed",
                                  "kernel_variant": args.variant},
                       "median_cost": float(cost.median())}), flush=True)
+
+
+def fd_fisher_throughput(eng, acts, args, param_ids=tuple(range(13)), delta=0.1, ksync=5):
+    """The reference's own excitation objective on the same candidates: the FD-Fisher episode
+    (1 main + 13 aux rollouts per candidate, aux at theta + 0.1 on one parameter, resync every 5
+    steps, trace(J^T J) of the finite differences after every step) over each candidate's whole
+    excitation, one fused launch (spi_fd_fisher)."""
+    import torch
+    from spi_gb300.active import fd_fisher
+    from spi_gb300.data import standing_state
+    from spi_gb300.robot import THETA_NOMINAL
+    n, T = acts.shape[:2]
+    x0 = torch.from_numpy(np.repeat(standing_state(1, z=0.32), n, 0)).cuda()
+    a = torch.from_numpy(acts).cuda()
+    th = THETA_NOMINAL.astype(np.float32)
+    obj = fd_fisher(eng, x0, a, th, param_ids, delta=delta, ksync=ksync)
+    torch.cuda.synchronize()
+    reps = max(1, min(args.steps, 5))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(eng.stream)
+    for _ in range(reps):
+        obj = fd_fisher(eng, x0, a, th, param_ids, delta=delta, ksync=ksync)
+    e1.record(eng.stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    o = obj.cpu().numpy()
+    rollout_steps = n * (len(param_ids) + 1) * (T + 1)
+    return {"workload": f"{n} candidates x (1 main + {len(param_ids)} aux) rollouts x {T + 1} control steps "
+                        f"(one zero-action reset step), delta {delta}, resync every {ksync} steps",
+            "ms": ms, "candidates_per_s": n / (ms * 1e-3), "rollout_steps_per_s": rollout_steps / (ms * 1e-3),
+            "objective_range": [float(np.min(o)), float(np.max(o))], "best_candidate": int(np.argmax(o))}
 
 
 def gradient_throughput(eng, args, n_theta=512, n_windows=256, horizon=20):
