@@ -325,16 +325,34 @@ def run_c3(args):
     cfg = eng.cfg
     n, wpc, H, settle = args.c3_candidates, 8, 20, 100
     acts, _ = multisine_actions(n, wpc * H, cfg.control_dt, cfg.action_scale, seed=3, settle=settle)
+    d_acts = torch.from_numpy(acts).cuda()            # the candidates stay resident on the device
     for _ in range(max(args.warmup, 1)):
-        r = score_excitations(eng, THETA_NOMINAL, acts, windows_per_cand=wpc, horizon=H, settle=settle)
+        r = score_excitations(eng, THETA_NOMINAL, d_acts, windows_per_cand=wpc, horizon=H, settle=settle)
     torch.cuda.synchronize()
-    times = []
+    times, parts = [], []
     with ClockSampler(0) as clocks:
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            r = score_excitations(eng, THETA_NOMINAL, acts, windows_per_cand=wpc, horizon=H, settle=settle)
+            tm = {}
+            r = score_excitations(eng, THETA_NOMINAL, d_acts, windows_per_cand=wpc, horizon=H, settle=settle,
+                                  timing=tm)
             torch.cuda.synchronize()
             times.append(time.perf_counter() - t0)
+            parts.append(tm)
+    breakdown = {k: float(np.mean([p[k] for p in parts])) for k in parts[0]}
+    # the sensitivity kernel against the FP32 peak: FP operations of the dual-number rollout (the
+    # kernel's formulation, one tangent, phase B once) per tangent rollout-step
+    from spi_gb300.engine import probe_fp32_peak
+    from spi_gb300.flops import dual_flops_per_rollout_step
+    dual_fl = dual_flops_per_rollout_step(cfg)
+    sens_roof = {"kernel": "sensitivity_kernel", "bound": "fp32",
+                 "achieved": n * wpc * H * 13 * dual_fl / (breakdown["sensitivities_ms"] * 1e-3) / 1e12,
+                 "peak": probe_fp32_peak() / 1e12, "unit": "TFLOP/s",
+                 "flops_per_tangent_rollout_step": dual_fl,
+                 "note": "achieved = tangent rollout-steps x FP operations of one dual-number control step "
+                         "(csrc/dual.cuh arithmetic, counted on the host; phase B once) / the sensitivity "
+                         "phase's device time; peak: the FP32 FMA-loop probe of this GPU"}
+    sens_roof["frac"] = sens_roof["achieved"] / sens_roof["peak"]
     # the Fisher reduction alone, tensor cores against CUDA cores, on the last Jacobians
     J, q = r["J"], block_weights((10.0, 5.0, 0.1, 0.1, 1.0, 0.01))
     fisher_ms = {}
@@ -375,7 +393,8 @@ def run_c3(args):
             "rollout_steps_per_s": (tangent_steps + primal_steps) / t,
             "tangent_rollout_steps_per_step": tangent_steps, "primal_rollout_steps_per_step": primal_steps,
             "fisher_ms": fisher_ms, "fisher_roofline": fisher_roof, "best_candidate": int(r["best"]),
-            "gradient": grad_line, "fd_fisher": fd_line,
+            "gradient": grad_line, "fd_fisher": fd_line, "breakdown_ms": breakdown,
+            "sensitivity_roofline": sens_roof,
             "logdet_range": [float(np.min(r["logdet"])), float(np.max(r["logdet"]))],
             "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)

@@ -46,6 +46,47 @@ inline Cf m_fabs(Cf x) { return Cf(std::fabs(x.v)); }
 inline Cf m_fmax(Cf a, Cf b) { return Cf(std::fmax(a.v, b.v)); }
 inline Cf m_fmin(Cf a, Cf b) { return Cf(std::fmin(a.v, b.v)); }
 
+// Counting dual number: value and one tangent, each operation as the device's forward-mode
+// scalar (dual.cuh) evaluates it, every + - * / sqrt tanh sin cos counted once.
+struct Cd {
+  Cf v, d;
+  Cd() {}
+  Cd(double x) : v(x), d(0.0) {}
+  Cd(float x) : v(x), d(0.0) {}
+  Cd(int x) : v(x), d(0.0) {}
+  Cd(Cf a, Cf b) : v(a), d(b) {}
+};
+inline Cd operator+(Cd a, Cd b) { return Cd(a.v + b.v, a.d + b.d); }
+inline Cd operator-(Cd a, Cd b) { return Cd(a.v - b.v, a.d - b.d); }
+inline Cd operator*(Cd a, Cd b) { return Cd(a.v * b.v, a.d * b.v + a.v * b.d); }
+inline Cd operator/(Cd a, Cd b) {
+  const Cf q = a.v / b.v;
+  return Cd(q, (a.d - q * b.d) / b.v);
+}
+inline Cd operator-(Cd a) { return Cd(-a.v, -a.d); }
+inline Cd& operator+=(Cd& a, Cd b) { a = a + b; return a; }
+inline Cd& operator-=(Cd& a, Cd b) { a = a - b; return a; }
+inline bool operator>(Cd a, Cd b) { return a.v > b.v; }
+inline bool operator<=(Cd a, Cd b) { return a.v <= b.v; }
+inline bool operator<(Cd a, Cd b) { return a.v < b.v; }
+inline Cd m_sqrt(Cd x) {
+  const Cf r = m_sqrt(x.v);
+  return Cd(r, r.v > 0 ? x.d * Cf(0.5) / r : Cf(0.0));
+}
+inline Cd m_tanh(Cd x) {
+  const Cf t = m_tanh(x.v);
+  return Cd(t, x.d * (Cf(1.0) - t * t));
+}
+inline void m_sincos(Cd x, Cd* s, Cd* c) {
+  Cf sv, cv;
+  m_sincos(x.v, &sv, &cv);
+  *s = Cd(sv, cv * x.d);
+  *c = Cd(cv, -sv * x.d);
+}
+inline Cd m_fabs(Cd x) { return x.v.v >= 0 ? x : Cd(-x.v, -x.d); }
+inline Cd m_fmax(Cd a, Cd b) { return a.v.v >= b.v.v ? a : b; }
+inline Cd m_fmin(Cd a, Cd b) { return a.v.v <= b.v.v ? a : b; }
+
 template <class T> static void add_out(LegOut<T>& a, const LegOut<T>& b) {
   add_to(a.I, b.I);
   a.p.w = a.p.w + b.p.w;
@@ -394,6 +435,27 @@ int spi_hostemu_grad(const spi_robot* robot, const double* init, const double* a
 int spi_hostemu_residual(const spi_robot* robot, const double* state, const double* theta, const double* act12,
                          double* out18) {
   return hostemu_residual(robot, state, theta, act12, out18);
+}
+
+// FP operations of one substep on the forward-mode dual scalar (value + one tangent), phase B
+// counted once: the work of one sensitivity direction per substep.
+int spi_hostemu_count_ops_dual(const spi_robot* robot, const double* state, const double* theta,
+                               const double* act12, long long* per_substep) {
+  DevModel M;
+  const char* why = "";
+  int rc = build_dev_model(*robot, &M, &why);
+  if (rc) return rc;
+  BaseState<Cd> B;
+  LegState<Cd> L[4];
+  BaseParams<Cd> bp;
+  LegParams<Cd> lp[4];
+  load_rollout(M, state, theta, B, L, bp, lp);
+  Cd act[12];
+  for (int j = 0; j < 12; ++j) act[j] = joint_target(M, j % 3, j / 3, Cd(act12[j]));
+  Cf::n = 0;
+  substep<false>(M, B, L, bp, lp, act);
+  *per_substep = Cf::n;
+  return SPI_OK;
 }
 
 // Algorithmic FP operations of one substep per phase: [A (all four legs), B (base), C (all legs)].

@@ -103,6 +103,9 @@ def hostemu_lib():
                                               POINTER(ctypes.c_longlong), POINTER(ctypes.c_longlong)]
         lib.spi_hostemu_count_ops_aba.restype = c_int
         lib.spi_hostemu_count_ops_aba.argtypes = lib.spi_hostemu_count_ops.argtypes
+        lib.spi_hostemu_count_ops_dual.restype = c_int
+        lib.spi_hostemu_count_ops_dual.argtypes = [POINTER(SpiRobot), c_void_p, c_void_p, c_void_p,
+                                                   POINTER(ctypes.c_longlong)]
         lib.spi_hostemu_grad.restype = c_int
         lib.spi_hostemu_grad.argtypes = [POINTER(SpiRobot), c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int,
                                          c_int, c_int, c_void_p, c_void_p]

@@ -8,6 +8,8 @@ base solve once):
   formulation, not by how the kernel evaluates it.
 * ``executed``: the kernel's own formulation (``csrc/dynamics.cuh``: each leg condensed through
   its joint-space inertia), which reaches the same result in fewer operations.
+* ``dual``: the kernel's formulation on the forward-mode dual scalar (value + one tangent, as
+  ``csrc/dual.cuh`` evaluates each operation): the work of one sensitivity direction.
 """
 from __future__ import annotations
 
@@ -58,3 +60,23 @@ def flops_per_rollout_step(cfg: SimConfig) -> int:
 
 def executed_flops_per_rollout_step(cfg: SimConfig) -> int:
     return cfg.decimation * executed_flops_per_substep(cfg)
+
+
+@lru_cache(maxsize=16)
+def _count_dual(cfg_key):
+    cfg = SimConfig(**dict(cfg_key))
+    r = to_struct(cfg)
+    x = np.ascontiguousarray(standing_state(1)[0], dtype=np.float64)
+    th = np.ascontiguousarray(THETA_NOMINAL, dtype=np.float64)
+    a = np.zeros(12, dtype=np.float64)
+    n = ctypes.c_longlong()
+    rc = _lib.hostemu_lib().spi_hostemu_count_ops_dual(ctypes.byref(r), x.ctypes.data, th.ctypes.data,
+                                                       a.ctypes.data, ctypes.byref(n))
+    if rc:
+        raise _lib.SpiError(rc, "dual flop count failed")
+    return n.value
+
+
+def dual_flops_per_rollout_step(cfg: SimConfig) -> int:
+    """FP operations of one control step of one sensitivity direction (dual scalar, phase B once)."""
+    return cfg.decimation * _count_dual(_key(cfg))

@@ -124,28 +124,43 @@ def multisine_actions(n_cand, T, control_dt, action_scale, n_comp=3, amp=(0.05, 
 
 
 def score_excitations(engine, theta, actions, windows_per_cand=8, horizon=20, settle=100, param_ids=None,
-                      sq_weights=(10.0, 5.0, 0.1, 0.1, 1.0, 0.01), eps=1e-9, tensor_cores=True):
+                      sq_weights=(10.0, 5.0, 0.1, 0.1, 1.0, 0.01), eps=1e-9, tensor_cores=True, timing=None):
     """Fisher scores of candidate excitations at theta.
 
-    actions [n_cand, settle + windows_per_cand * horizon, 12]. Each candidate is rolled from a
-    standing start; windows of `horizon` steps start every `horizon` steps after `settle`.
-    Returns dict(logdet [n], trace [n], best, F [n,K,K]).
+    actions [n_cand, settle + windows_per_cand * horizon, 12] (host array or device tensor; a
+    device tensor stays on the device). Each candidate is rolled from a standing start; windows
+    of `horizon` steps start every `horizon` steps after `settle`. Returns dict(logdet [n],
+    trace [n], best, F [n,K,K], J). timing: a dict that receives the device time in ms of the
+    settle trace, the sensitivities and the Fisher reduction (CUDA events on the engine stream).
     """
     param_ids = list(range(THETA_DIM)) if param_ids is None else list(param_ids)
-    actions = np.asarray(actions, np.float32)
-    n, T = actions.shape[:2]
-    theta = np.asarray(theta, np.float32).reshape(1, THETA_DIM)
-    x0 = standing_state(n)
-    engine.load_windows(torch.from_numpy(x0), torch.from_numpy(actions), torch.from_numpy(x0))
-    _, _, tr = engine.evaluate(torch.from_numpy(theta), trace=True)          # [1, n, T, 37]
+    dev = engine.device
+    acts = torch.as_tensor(actions, dtype=torch.float32, device=dev)
+    n, T = int(acts.shape[0]), int(acts.shape[1])
+    th = torch.as_tensor(np.asarray(theta, np.float32).reshape(1, THETA_DIM), device=dev)
+    x0 = torch.from_numpy(standing_state(n)).to(dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)] if timing is not None else None
+    if ev:
+        ev[0].record(engine.stream)
+    engine.load_windows(x0, acts, x0)
+    _, _, tr = engine.evaluate(th, trace=True)                                # [1, n, T, 37]
     tr = tr[0]
     starts = settle - 1 + horizon * np.arange(windows_per_cand)               # state index before each window
-    idx = torch.as_tensor(starts, device=tr.device)
-    init = tr[:, idx].reshape(-1, STATE_DIM)                                  # [n * wpc, 37]
-    act = torch.from_numpy(np.stack([actions[:, s + 1:s + 1 + horizon] for s in starts], 1)).reshape(-1, horizon, 12)
+    init = tr[:, torch.as_tensor(starts, device=dev)].reshape(-1, STATE_DIM)  # [n * wpc, 37]
+    steps = torch.as_tensor(starts[:, None] + 1 + np.arange(horizon)[None, :], device=dev)
+    act = acts[:, steps].reshape(-1, horizon, 12)                              # [n * wpc, H, 12]
+    if ev:
+        ev[1].record(engine.stream)
     engine.load_windows(init, act, init)
-    J, _ = sensitivities(engine, torch.from_numpy(theta), param_ids)          # [1, n*wpc, 37, K]
+    J, _ = sensitivities(engine, th, param_ids)                               # [1, n*wpc, 37, K]
     J = J.reshape(n, windows_per_cand, STATE_DIM, len(param_ids))
+    if ev:
+        ev[2].record(engine.stream)
     F, logdet, trace = fisher(J, block_weights(sq_weights), eps, tensor_cores=tensor_cores)
+    if ev:
+        ev[3].record(engine.stream)
     ld = logdet.cpu().numpy()
+    if ev:
+        timing.update(settle_trace_ms=ev[0].elapsed_time(ev[1]), sensitivities_ms=ev[1].elapsed_time(ev[2]),
+                      fisher_ms=ev[2].elapsed_time(ev[3]))
     return {"logdet": ld, "trace": trace.cpu().numpy(), "best": int(np.argmax(ld)), "F": F, "J": J}

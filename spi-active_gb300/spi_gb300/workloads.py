@@ -87,8 +87,9 @@ class FisherScorer:
         self.stream = torch.cuda.Stream(device=device) if own_stream else None
         self.engine = Engine(cfg, device=device, stream=self.stream)
         c = self.engine.cfg
-        self.actions, _ = multisine_actions(FISHER_CANDIDATES, FISHER_WINDOWS * FISHER_H, c.control_dt,
-                                            c.action_scale, seed=11, settle=100)
+        acts, _ = multisine_actions(FISHER_CANDIDATES, FISHER_WINDOWS * FISHER_H, c.control_dt, c.action_scale,
+                                    seed=11, settle=100)
+        self.actions = torch.from_numpy(acts).to(self.engine.device)   # resident on the device
 
     def score(self, theta):
         from .sensitivity import score_excitations
