@@ -86,3 +86,32 @@ def test_model_builder_rejects_unsupported_joint_origins(built):
         r = to_struct(SimConfig())
         r.foot[comp] = 0.01
         assert run(r) == -1, comp
+
+
+def test_gradient_fd_fisher_and_search_entry_points_validate_arguments(built):
+    """spi_adjoint, spi_fd_fisher and spi_search_* refuse null handles and out-of-range sizes with
+    SPI_EINVAL before any CUDA call (no GPU needed)."""
+    import ctypes
+    from spi_gb300 import _lib
+    from spi_gb300.cem import SpiCemConfig
+    lib = _lib.engine_lib()
+    assert lib.spi_adjoint(None, None, 4, None, None) == -1
+    assert b"spi_adjoint" in lib.spi_last_error()
+    ids = (ctypes.c_int32 * 2)(0, 1)
+    assert lib.spi_fd_fisher(None, None, None, None, 4, 10, ids, 2, 0.1, 5, 1, None, None) == -1
+    assert b"spi_fd_fisher" in lib.spi_last_error()
+    out = ctypes.c_void_p()
+    cfg = SpiCemConfig()
+    cfg.n_samples, cfg.dim = 1, 2          # fewer than two samples
+    assert lib.spi_search_create(ctypes.byref(cfg), None, ctypes.byref(out)) == -1
+    assert b"n_samples" in lib.spi_last_error()
+    cfg.n_samples, cfg.dim = 64, 14        # more than 13 dimensions
+    assert lib.spi_search_create(ctypes.byref(cfg), None, ctypes.byref(out)) == -1
+    cfg.dim = 2
+    cfg.param_ids[0], cfg.param_ids[1] = 3, 3
+    cfg.lo[0], cfg.hi[0], cfg.lo[1], cfg.hi[1] = 0.0, 1.0, 0.0, 1.0
+    cfg.elite_frac, cfg.alpha = 0.1, 1.0
+    assert lib.spi_search_create(ctypes.byref(cfg), None, ctypes.byref(out)) == -1   # repeated slot
+    assert b"repeated" in lib.spi_last_error()
+    assert lib.spi_search_sample(None, None) == -1
+    assert lib.spi_search_refit(None, None) == -1
