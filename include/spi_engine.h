@@ -243,7 +243,8 @@ int spi_search_read(spi_search* s, double* mu, double* cov, float* best, float* 
  * excitations at once: spigym/envs/sysid/active_sysid_openloop.py:29-80 (each candidate is a
  * group of 1 main + P aux rollouts, aux k at theta + delta on slot param_ids[k]), :246-252 and
  * :316-330 (after 1-based control step t with t % ksync == 1, or after every step when
- * ksync <= 1, the aux rollouts take the main's state) and :402-426 (after every step the reward
+ * 0 <= ksync <= 1, the aux rollouts take the main's state; never when ksync < 0) and :402-426
+ * (after every step the reward
  * trace(J^T J), J = (s_main - s_aux) / delta over the 13 root-state entries and 12 joint
  * positions). x0 device [C][37] start states, actions device [C][T][12], theta device [C][13]
  * (each group's main theta), param_ids host [P] (P <= 13, distinct slots). reward_sum device

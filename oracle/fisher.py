@@ -50,8 +50,8 @@ def fd_fisher_episode(x0, actions, theta, param_ids, delta, ksync, sim, reset_st
       step_idx = 1 after it, before the policy loop (reset_step);
     * per step (_pre_physics_step :170-172 increments step_idx; _post_physics_step
       :209-252): the reward ``fd_fisher_reward`` of the new states, then, when
-      step_idx % ksync == 1 (every step if ksync <= 1), the aux states set to the main's
-      (_reset_envs_states_to_main_envs :316-330);
+      step_idx % ksync == 1 (every step if 0 <= ksync <= 1, never if ksync < 0), the aux
+      states set to the main's (_reset_envs_states_to_main_envs :316-330);
     * evaluate_policy (active_sysid.py:527-600): rewards of the loop steps summed and divided
       by the loop's step counter, which ends one above the number of steps.
 
@@ -75,7 +75,7 @@ def fd_fisher_episode(x0, actions, theta, param_ids, delta, ksync, sim, reset_st
         return fd_fisher_reward(xs[:, :13], xs[:, 13:25], origins, C, P, delta)[main]
 
     def resync(xs, step_idx):
-        if ksync <= 1 or step_idx % ksync == 1:
+        if ksync >= 0 and (ksync <= 1 or step_idx % ksync == 1):
             xs = xs.copy()
             for k in range(1, G):
                 xs[main + k] = xs[main]

@@ -147,9 +147,10 @@ __global__ void __launch_bounds__(128) fd_fisher_kernel(const DevModel* __restri
       if (t >= a.skip) total += R;
       if (a.reward_trace) a.reward_trace[(size_t)cand * a.T + t] = R;
     }
-    // resync: aux <- main after 1-based step t + 1 when (t + 1) % ksync == 1 (every step if ksync <= 1)
+    // resync: aux <- main after 1-based step t + 1 when (t + 1) % ksync == 1 (every step if
+    // 0 <= ksync <= 1, never if ksync < 0)
     const int step = t + 1;
-    if (a.ksync <= 1 || step % a.ksync == 1) {
+    if (a.ksync >= 0 && (a.ksync <= 1 || step % a.ksync == 1)) {
       if (valid && member == 0) {
         float* d = xs[grp];
         if (leg == 0) base_pack(B, d);

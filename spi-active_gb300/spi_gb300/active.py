@@ -42,7 +42,14 @@ def fd_fisher(engine, x0, actions, theta, param_ids, delta=0.1, ksync=5, reset_s
     x0 [C, 37] start states, actions [C, n, 12] raw actions, theta [13] or [C, 13] (each group's
     main), param_ids the theta slots of the aux rollouts (P <= 13). Returns the objective [C]
     (reward sum over the n loop steps / (n + 1)) as a device tensor, and with ``trace`` also the
-    per-step rewards [C, n]."""
+    per-step rewards [C, n].
+
+    ksync: the aux rollouts take the main's state every ksync steps, as the reference's docstrings
+    and config describe (`_reset_envs_states_to_main_envs`); ksync < 0 never resyncs. The
+    reference writes that resync into the simulator's state-tensor views only, without the
+    set_actor_root_state_tensor / set_dof_state_tensor call that pushes them to the simulator,
+    and the next refresh overwrites the views; under Isaac Gym its aux envs may therefore never
+    be resynced, which is what ksync < 0 reproduces."""
     dev = engine.device
     actions = torch.as_tensor(actions, dtype=torch.float32, device=dev)
     C, n = int(actions.shape[0]), int(actions.shape[1])

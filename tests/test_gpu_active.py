@@ -27,7 +27,7 @@ def _case(C, n, seed):
 
 
 @pytest.mark.parametrize("param_ids,ksync,delta", [([0, 1], 5, 0.1), (list(range(13)), 1, 0.1),
-                                                   ([0, 4, 7, 10], 3, 0.05)])
+                                                   ([0, 4, 7, 10], 3, 0.05), ([0, 2], -1, 0.1)])
 def test_fd_fisher_matches_oracle_episode(built, param_ids, ksync, delta):
     from spi_gb300.active import fd_fisher
     from spi_gb300.engine import Engine
