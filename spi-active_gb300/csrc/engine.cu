@@ -1,16 +1,17 @@
 // engine.cu -- C ABI of the batched candidate-evaluation engine (declared in spi_engine.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
 
 #include "common.h"
+#include "engine_impl.h"
+#include "items.h"
 #include "model.h"
 #include "rollout.cuh"
 #include "rollout_block.cuh"
-#include "rollout_lane.cuh"
-#include "engine_impl.h"
 
 using namespace spi;
 
@@ -50,6 +51,17 @@ __global__ void fill_f32(float* p, float v, long long n) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
 }
+// Resident CTAs of the engine's persistent rollout kernel (layout, min_blocks) on this device.
+int update_item_ctas(spi_engine* e) {
+  if (e->layout != SPI_LAYOUT_LANE && e->layout != SPI_LAYOUT_QUAD) return SPI_OK;
+  int dev = 0, sms = 0, occ = 0;
+  cudaError_t ce = cudaGetDevice(&dev);
+  if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (ce == cudaSuccess) ce = items_occupancy(e->layout, e->min_blocks, &occ);
+  if (ce != cudaSuccess) return cuda_error(ce, "rollout kernel occupancy");
+  e->item_ctas = sms * std::max(occ, 1);
+  return SPI_OK;
+}
 }  // namespace
 
 int spi::run_impl(spi_engine* e, float* trace) {
@@ -68,24 +80,26 @@ int spi::run_impl(spi_engine* e, float* trace) {
   const long long warps = (long long)e->N * G;
   const unsigned grid = blocks_for(warps, 4);
   unsigned long long* bad = (unsigned long long*)e->bad.p;
-  if (!trace && e->layout == SPI_LAYOUT_LANE) {
-    const long long lwarps = ((long long)e->N * G + 3) / 4;   // four (theta, 8-window group) items a warp
-    const unsigned lgrid = blocks_for(lwarps, 4);
-    if (e->min_blocks <= 2)
-      rollout_lane_kernel<2><<<lgrid, 128, kLaneParkBytes, e->stream>>>(e->host_model, win, e->theta.f(), e->N, G,
-                                                                        e->partial.f(), bad);
-    else if (e->min_blocks == 3 && motor_shape_of(e->host_model) == kMotorSpeedLimit)
-      rollout_lane_kernel<3, kMotorSpeedLimit><<<lgrid, 128, kLaneParkBytes, e->stream>>>(
-          e->host_model, win, e->theta.f(), e->N, G, e->partial.f(), bad);
-    else if (e->min_blocks == 3)
-      rollout_lane_kernel<3><<<lgrid, 128, kLaneParkBytes, e->stream>>>(e->host_model, win, e->theta.f(), e->N, G,
-                                                                        e->partial.f(), bad);
-    else if (motor_shape_of(e->host_model) == kMotorSpeedLimit)
-      rollout_lane_kernel<4, kMotorSpeedLimit><<<lgrid, 128, kLaneParkBytes, e->stream>>>(
-          e->host_model, win, e->theta.f(), e->N, G, e->partial.f(), bad);
-    else
-      rollout_lane_kernel<4><<<lgrid, 128, kLaneParkBytes, e->stream>>>(e->host_model, win, e->theta.f(), e->N, G,
-                                                                        e->partial.f(), bad);
+  if (!trace && (e->layout == SPI_LAYOUT_LANE || e->layout == SPI_LAYOUT_QUAD)) {
+    // the server's persistent kernel on a table of one slot (items.h)
+    SlotDesc d{};
+    d.win = win;
+    d.theta = e->theta.f();
+    d.partial = e->partial.f();
+    d.comp = e->comp.f();
+    d.cost = e->cost.f();
+    d.N = e->N;
+    d.G = G;
+    d.norm = e->norm;
+    d.active = 1;
+    const long long items = items_of(e->layout, e->N, G);
+    const int ctas = (int)std::min<long long>((items + 3) / 4, std::max(e->item_ctas, 1));
+    SingleTable* tab = static_cast<SingleTable*>(e->items.p);
+    cudaError_t ce = items_fill_single(tab, d, items, 1, e->stream);
+    if (ce == cudaSuccess)
+      ce = items_launch(e->layout, e->min_blocks, e->host_model, e->d_model, single_tables(tab), 0, ctas, bad,
+                        e->stream);
+    if (ce != cudaSuccess) return cuda_error(ce, "rollout launch");
   } else if (!trace && e->layout == SPI_LAYOUT_BLOCK) {
     if (e->min_blocks == 4)
       rollout_block_kernel<4><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
@@ -96,18 +110,10 @@ int spi::run_impl(spi_engine* e, float* trace) {
     else
       rollout_block_kernel<3><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
                                                             e->partial.f(), bad);
-  } else if (trace)
+  } else {
     rollout_kernel<true, 3><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
                                                          e->partial.f(), trace, bad);
-  else if (e->min_blocks == 4)
-    rollout_kernel<false, 4><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
-                                                          e->partial.f(), nullptr, bad);
-  else if (e->min_blocks == 5)
-    rollout_kernel<false, 5><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
-                                                          e->partial.f(), nullptr, bad);
-  else
-    rollout_kernel<false, 3><<<grid, 128, 0, e->stream>>>(e->d_model, win, e->theta.f(), e->N, G,
-                                                          e->partial.f(), nullptr, bad);
+  }
   cudaError_t ce = cudaGetLastError();
   if (ce != cudaSuccess) return cuda_error(ce, "rollout_kernel launch");
   const float* w = e->sq_w;
@@ -139,6 +145,7 @@ int spi_create(const spi_robot* robot, spi_engine** out) {
   ce = cudaMemcpy(e->d_model, &e->host_model, sizeof(DevModel), cudaMemcpyHostToDevice);
   if (ce != cudaSuccess) { cudaFree(e->d_model); delete e; return cuda_error(ce, "spi_create: upload model"); }
   rc = e->bad.reserve(sizeof(unsigned long long));
+  if (!rc) rc = e->items.reserve(sizeof(SingleTable));
   if (rc) { cudaFree(e->d_model); delete e; return rc; }
   cudaMemset(e->bad.p, 0, sizeof(unsigned long long));
   // default kernel: the lane layout at the 128-register cap (the fastest on the C1 workload)
@@ -216,7 +223,7 @@ int spi_set_kernel_config(spi_engine* e, int min_blocks) {
     return set_error(SPI_EINVAL, "spi_set_kernel_config: min_blocks %d outside [%d, 5]", min_blocks, lo);
   e->min_blocks = min_blocks;
   if (e->graph_exec) { cudaGraphExecDestroy(e->graph_exec); e->graph_exec = nullptr; }
-  return SPI_OK;
+  return update_item_ctas(e);
 }
 
 int spi_set_kernel_layout(spi_engine* e, int layout) {
@@ -225,27 +232,14 @@ int spi_set_kernel_layout(spi_engine* e, int layout) {
     return set_error(SPI_EINVAL, "spi_set_kernel_layout: layout %d not 0/1/2", layout);
   if (layout == SPI_LAYOUT_LANE) {
     // the parking area is above the 48 KB default for dynamic shared memory
-    cudaError_t ce = cudaFuncSetAttribute(rollout_lane_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          kLaneParkBytes);
-    if (ce == cudaSuccess)
-      ce = cudaFuncSetAttribute(rollout_lane_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                kLaneParkBytes);
-    if (ce == cudaSuccess)
-      ce = cudaFuncSetAttribute(rollout_lane_kernel<3, kMotorSpeedLimit>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, kLaneParkBytes);
-    if (ce == cudaSuccess)
-      ce = cudaFuncSetAttribute(rollout_lane_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                kLaneParkBytes);
-    if (ce == cudaSuccess)
-      ce = cudaFuncSetAttribute(rollout_lane_kernel<4, kMotorSpeedLimit>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, kLaneParkBytes);
+    const cudaError_t ce = items_prepare_lane();
     if (ce != cudaSuccess) return cuda_error(ce, "spi_set_kernel_layout: shared-memory attribute");
   } else if (e->min_blocks < 3) {
     e->min_blocks = 3;
   }
   e->layout = layout;
   if (e->graph_exec) { cudaGraphExecDestroy(e->graph_exec); e->graph_exec = nullptr; }
-  return SPI_OK;
+  return update_item_ctas(e);
 }
 
 int spi_set_cost(spi_engine* e, int mode, const float* sq_weights) {

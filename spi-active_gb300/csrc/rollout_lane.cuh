@@ -218,22 +218,4 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
   }
 }
 
-// One warp per four (theta, eight-window group) items; grid covers ceil(N G / 4) warps, G =
-// ceil(W / 8) (the partial layout's window groups). CTAs of 128 threads with
-// kLaneParkBytes of dynamic shared memory. MINB sets the register cap (2: ~200, 3: 168, 4: 128);
-// shared memory holds every variant to three CTAs per SM, and at 128 registers the code still
-// needs no spills.
-template <int MINB, int MS = kMotorRuntime>
-__global__ void __launch_bounds__(128, MINB) rollout_lane_kernel(const __grid_constant__ DevModel M, WinView win,
-                                                                 const float* __restrict__ theta, int N, int G,
-                                                                 float* __restrict__ partial,
-                                                                 unsigned long long* __restrict__ n_bad) {
-  extern __shared__ float4 lane_smem[];              // kLaneParkBytes
-  __shared__ BaseParams<float> bp_warp[4][4];
-  __shared__ float4 gains_warp[4][4][8];
-  const long long warp = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (warp * 4 >= (long long)N * G) return;   // uniform per warp
-  rollout_lane_warp<MS>(M, win, theta, warp * 4, N, partial, G, n_bad, lane_smem, bp_warp, gains_warp);
-}
-
 }  // namespace spi

@@ -2,9 +2,10 @@
 //
 // Slots hold admitted jobs (windows in SoA layout, population, cost partials, CEM state).
 // A tick advances every active slot by one CEM iteration:
-//   memset(work counter) -> cem_sample_kernel (grid row per slot) -> server_rollout_kernel
-//   (persistent; each warp claims (slot, theta, 8-window group) work items from an atomic
-//   counter, ordered longest horizon first) -> server_finalize_kernel -> cem_refit_kernel.
+//   memset(work counter) -> cem_sample_kernel (grid row per slot) -> the persistent rollout
+//   kernel of items.cu (each warp claims (slot, theta, 8-window group) work items from an
+//   atomic counter, ordered longest horizon first; the single-job engine launches the same
+//   kernel on a one-slot table) -> server_finalize_kernel -> cem_refit_kernel.
 // The tick is captured once as a CUDA graph: every per-tick quantity (slot table, work
 // order, item count) lives in device buffers that the host refreshes before each launch.
 #include <cuda_runtime.h>
@@ -16,36 +17,19 @@
 
 #include "cem.cuh"
 #include "common.h"
+#include "items.h"
 #include "model.h"
 #include "rollout.cuh"
-#include "rollout_lane.cuh"
 
 using namespace spi;
 
 namespace {
-
-struct SlotDesc {
-  WinView win;
-  float* theta;
-  float* partial;
-  float* comp;
-  float* cost;
-  int N, G;
-  float norm;
-  int active;
-};
 
 // A tick runs up to kMaxRounds rounds of one CEM iteration each (sample, rollout, finalize,
 // refit); slot j takes part in rounds 0 .. rounds[j] - 1, so jobs with less work per
 // iteration advance several iterations per tick. Per round the rollout's work items are
 // laid out slot after slot (begin[round][slot]) in the order order[round][0 .. n_order).
 constexpr int kMaxRounds = 8;
-
-struct TickInfo {
-  long long total;   // work items this tick
-  int n_order;       // active slots in `order`
-  int items_per_claim;
-};
 
 struct SlotHost {
   bool used = false;      // holds a job (or its unread result)
@@ -77,91 +61,6 @@ __global__ void srv_actions_to_hw(const float* __restrict__ src, float* __restri
 __global__ void srv_fill(float* p, float v, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
-}
-
-// Persistent rollout over the work items of every active slot.
-template <int MINB>
-__global__ void __launch_bounds__(128, MINB) server_rollout_kernel(const DevModel* __restrict__ model,
-                                                             const SlotDesc* __restrict__ slots,
-                                                             const int* __restrict__ order_all,
-                                                             const long long* __restrict__ begin_all,
-                                                             const TickInfo* __restrict__ info_all,
-                                                             unsigned long long* __restrict__ counter_all,
-                                                             unsigned long long* __restrict__ n_bad,
-                                                             int max_slots, int round) {
-  __shared__ DevModel M;
-  load_model_smem(&M, model);
-  __syncthreads();
-  const int lane = threadIdx.x & 31;
-  const TickInfo* info = info_all + round;
-  const int* order = order_all + (size_t)round * max_slots;
-  const long long* begin = begin_all + (size_t)round * max_slots;
-  unsigned long long* counter = counter_all + round;
-  const long long total = info->total;
-  const int n_order = info->n_order, per = info->items_per_claim;
-  while (true) {
-    unsigned long long first = 0;
-    if (lane == 0) first = atomicAdd(counter, (unsigned long long)per);
-    first = __shfl_sync(0xffffffffu, first, 0);
-    if ((long long)first >= total) break;
-    for (int k = 0; k < per; ++k) {
-      const long long item = (long long)first + k;
-      if (item >= total) break;
-      int lo = 0, hi = n_order - 1;   // last slot whose range starts at or before item
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (begin[order[mid]] <= item) lo = mid; else hi = mid - 1;
-      }
-      const SlotDesc& S = slots[order[lo]];
-      const long long local = item - begin[order[lo]];
-      const int n = (int)(local / S.G), g = (int)(local % S.G);
-      rollout_group<false>(M, S.win, S.theta + (size_t)n * SPI_THETA_DIM, g,
-                           S.partial + ((size_t)n * S.G + g) * SPI_N_COMP, nullptr, n_bad);
-    }
-  }
-}
-
-// The same in the lane layout: each work item is four (theta, 8-window group) items of one slot,
-// one lane per window through all four legs (rollout_lane_warp). CTAs of 128 threads with kLaneParkBytes
-// of dynamic shared memory; the model by value; MS its motor shape.
-template <int MINB, int MS = kMotorRuntime>
-__global__ void __launch_bounds__(128, MINB) server_rollout_lane_kernel(const __grid_constant__ DevModel M,
-                                                                  const SlotDesc* __restrict__ slots,
-                                                                  const int* __restrict__ order_all,
-                                                                  const long long* __restrict__ begin_all,
-                                                                  const TickInfo* __restrict__ info_all,
-                                                                  unsigned long long* __restrict__ counter_all,
-                                                                  unsigned long long* __restrict__ n_bad,
-                                                                  int max_slots, int round) {
-  extern __shared__ float4 lane_smem[];              // kLaneParkBytes
-  __shared__ BaseParams<float> bp_warp[4][4];
-  __shared__ float4 gains_warp[4][4][8];
-  const int lane = threadIdx.x & 31;
-  const TickInfo* info = info_all + round;
-  const int* order = order_all + (size_t)round * max_slots;
-  const long long* begin = begin_all + (size_t)round * max_slots;
-  unsigned long long* counter = counter_all + round;
-  const long long total = info->total;
-  const int n_order = info->n_order, per = info->items_per_claim;
-  while (true) {
-    unsigned long long first = 0;
-    if (lane == 0) first = atomicAdd(counter, (unsigned long long)per);
-    first = __shfl_sync(0xffffffffu, first, 0);
-    if ((long long)first >= total) break;
-    for (int k = 0; k < per; ++k) {
-      const long long item = (long long)first + k;
-      if (item >= total) break;
-      int lo = 0, hi = n_order - 1;   // last slot whose range starts at or before item
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (begin[order[mid]] <= item) lo = mid; else hi = mid - 1;
-      }
-      const SlotDesc& S = slots[order[lo]];
-      const long long local = item - begin[order[lo]];
-      rollout_lane_warp<MS>(M, S.win, S.theta, local * 4, S.N, S.partial, S.G, n_bad, lane_smem, bp_warp,
-                            gains_warp);
-    }
-  }
 }
 
 __global__ void server_finalize_kernel(const SlotDesc* __restrict__ slots, const int* __restrict__ rounds, int round,
@@ -237,10 +136,7 @@ namespace {
 
 // Work items of one slot per tick: (theta, 8-window group) in the quad layout, four of them (a
 // warp's worth) in the lane layout.
-long long slot_items(const spi_server* s, const SlotDesc& d) {
-  const long long groups = (long long)d.N * d.G;
-  return s->layout == SPI_LAYOUT_LANE ? (groups + 3) / 4 : groups;
-}
+long long slot_items(const spi_server* s, const SlotDesc& d) { return items_of(s->layout, d.N, d.G); }
 
 bool server_busy(const spi_server* s) {
   for (const auto& sl : s->slots)
@@ -277,30 +173,9 @@ int enqueue_tick(spi_server* s) {
   const float* w = s->sq_w;
   for (int r = 0; r < s->rounds; ++r) {
     cem_sample_kernel<<<dim3(rows, s->max_slots), 128, 0, s->stream>>>(s->d_cem, s->d_rounds, r);
-    if (s->layout == SPI_LAYOUT_LANE) {
-      const bool sl = motor_shape_of(s->host_model) == kMotorSpeedLimit;
-      if (s->min_blocks <= 2)
-        server_rollout_lane_kernel<2><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
-            s->host_model, s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
-      else if (s->min_blocks == 3 && sl)
-        server_rollout_lane_kernel<3, kMotorSpeedLimit><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
-            s->host_model, s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
-      else if (s->min_blocks == 3)
-        server_rollout_lane_kernel<3><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
-            s->host_model, s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
-      else if (sl)
-        server_rollout_lane_kernel<4, kMotorSpeedLimit><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
-            s->host_model, s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
-      else
-        server_rollout_lane_kernel<4><<<s->grid, 128, kLaneParkBytes, s->stream>>>(
-            s->host_model, s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
-    } else if (s->min_blocks == 4) {
-      server_rollout_kernel<4><<<s->grid, 128, 0, s->stream>>>(s->d_model, s->d_slots, s->d_order, s->d_begin,
-                                                               s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
-    } else {
-      server_rollout_kernel<3><<<s->grid, 128, 0, s->stream>>>(s->d_model, s->d_slots, s->d_order, s->d_begin,
-                                                               s->d_info, s->d_counter, s->d_bad, s->max_slots, r);
-    }
+    const ItemTables t{s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->max_slots};
+    ce = items_launch(s->layout, s->min_blocks, s->host_model, s->d_model, t, r, s->grid, s->d_bad, s->stream);
+    if (ce != cudaSuccess) return cuda_error(ce, "tick: rollout launch");
     server_finalize_kernel<<<dim3(rows, s->max_slots), 128, 0, s->stream>>>(s->d_slots, s->d_rounds, r, s->cost_mode,
                                                                             w[0], w[1], w[2], w[3], w[4], w[5]);
     cem_refit_kernel<<<s->max_slots, 1024, npad * sizeof(unsigned long long), s->stream>>>(s->d_cem, s->d_rounds, r);
@@ -331,17 +206,7 @@ int resize_grid(spi_server* s) {
   int dev = 0, sms = 0, occ = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaError_t ce;
-  if (s->layout == SPI_LAYOUT_LANE)
-    ce = s->min_blocks <= 2   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_lane_kernel<2>, 128,
-                                                                                kLaneParkBytes)
-         : s->min_blocks == 3 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_lane_kernel<3>, 128,
-                                                                                kLaneParkBytes)
-                              : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_lane_kernel<4>, 128,
-                                                                                kLaneParkBytes);
-  else
-    ce = s->min_blocks == 4 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_kernel<4>, 128, 0)
-                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, server_rollout_kernel<3>, 128, 0);
+  const cudaError_t ce = items_occupancy(s->layout, s->min_blocks, &occ);
   if (ce != cudaSuccess) return cuda_error(ce, "server: occupancy");
   const int per = s->ctas_per_sm > 0 ? std::min(s->ctas_per_sm, std::max(occ, 1)) : std::max(occ, 1);
   s->grid = sms * per;
@@ -474,20 +339,7 @@ int spi_server_set_kernel_layout(spi_server* s, int layout) {
   if (server_busy(s))
     return set_error(SPI_ESTATE, "spi_server_set_kernel_layout: jobs in flight");
   if (layout == SPI_LAYOUT_LANE) {
-    cudaError_t ce = cudaFuncSetAttribute(server_rollout_lane_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          kLaneParkBytes);
-    if (ce == cudaSuccess)
-      ce = cudaFuncSetAttribute(server_rollout_lane_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                kLaneParkBytes);
-    if (ce == cudaSuccess)
-      ce = cudaFuncSetAttribute(server_rollout_lane_kernel<3, kMotorSpeedLimit>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, kLaneParkBytes);
-    if (ce == cudaSuccess)
-      ce = cudaFuncSetAttribute(server_rollout_lane_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                kLaneParkBytes);
-    if (ce == cudaSuccess)
-      ce = cudaFuncSetAttribute(server_rollout_lane_kernel<4, kMotorSpeedLimit>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, kLaneParkBytes);
+    const cudaError_t ce = items_prepare_lane();
     if (ce != cudaSuccess) return cuda_error(ce, "spi_server_set_kernel_layout: shared-memory attribute");
     s->min_blocks = std::min(std::max(s->min_blocks, 2), 4);
   } else {

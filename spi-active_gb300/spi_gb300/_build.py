@@ -21,7 +21,7 @@ LIB_DIR = PKG / "_lib"
 ENGINE_SO = LIB_DIR / "libspi_engine.so"
 HOSTEMU_SO = LIB_DIR / "libspi_hostemu.so"
 
-CU_SOURCES = ("engine.cu", "cem.cu", "server.cu", "sensitivity.cu", "step.cu", "probe.cu", "noalloc.cu", "fd_fisher.cu", "search.cu", "adjoint.cu")
+CU_SOURCES = ("engine.cu", "items.cu", "cem.cu", "server.cu", "sensitivity.cu", "step.cu", "probe.cu", "noalloc.cu", "fd_fisher.cu", "search.cu", "adjoint.cu")
 ARCH = ("-gencode", "arch=compute_103a,code=sm_103a")
 NVCC_FLAGS = ARCH + ("-O3", "-lineinfo", "-std=c++17", "-ftz=true", "-prec-div=false", "-prec-sqrt=false",
                      "-Xcompiler", "-fPIC",

@@ -47,7 +47,7 @@ def _bind(lib):
 class CEM:
     """CEM identification of ``param_ids`` (theta slots) on an engine with loaded windows."""
 
-    launches_per_step = 4   # sample, rollout, cost finalize, refit
+    launches_per_step = 5   # sample, rollout-table fill, rollout, cost finalize, refit
 
     def __init__(self, engine, n_samples, param_ids, lo, hi, nominal, elite_frac=0.1, alpha=1.0,
                  min_std_frac=1e-3, seed=0, job_id=0):

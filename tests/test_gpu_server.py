@@ -43,30 +43,69 @@ def test_same_result_alone_and_in_the_mix(built, variant):
         assert np.array_equal(r["mu"], alone["mu"])
 
 
-@pytest.mark.parametrize("variant", ["quad3", "lane4"])
-def test_server_job_equals_engine_cem(built, variant):
-    """A server job and the single-job engine CEM agree within the 1e-4 relative cost bar.
-
-    The rollouts are the same code; the two cost-finalize kernels may contract the weighted
-    sum into FMAs differently, so the last bits of a cost can differ.
-    """
+def _engine_cem(variant, init, actions, target, n, ids, seed, job_id, iters):
+    from spi_gb300.autotune import set_variant
     from spi_gb300.cem import CEM
     from spi_gb300.engine import Engine
-    from spi_gb300.server import Server
-    ids = [0, 1, 2, 4]
-    job, (init, actions, target) = _job(4, 32, 6, 128, ids, 21, iters=5)
-    r = _run(_server(variant, max_slots=4, max_samples=128), [(job, None)])[21]
-    from spi_gb300.autotune import set_variant
     e = Engine()
     e.load_windows(init, actions, target)
     set_variant(e, variant)
-    cem = CEM(e, n_samples=128, param_ids=ids, lo=gm.THETA_PRIOR_LO[ids], hi=gm.THETA_PRIOR_HI[ids],
-              nominal=gm.THETA_NOMINAL, seed=104, job_id=21)
-    for _ in range(5):
-        cem.step()
-    ref = cem.read()
-    np.testing.assert_allclose(r["mu"], ref["mu"], rtol=1e-6)
-    assert abs(ref["best_cost"] - r["best_cost"]) <= 1e-4 * abs(ref["best_cost"])
+    cem = CEM(e, n_samples=n, param_ids=ids, lo=gm.THETA_PRIOR_LO[ids], hi=gm.THETA_PRIOR_HI[ids],
+              nominal=gm.THETA_NOMINAL, seed=seed, job_id=job_id)
+    cem.run(iters, graph=True)
+    return cem.read()
+
+
+def _assert_same(r, ref):
+    assert r["iterations"] == ref["iteration"]
+    assert r["best_cost"] == ref["best_cost"], (r["best_cost"], ref["best_cost"])
+    assert np.array_equal(r["best_theta"], ref["best_theta"])
+    assert np.array_equal(r["mu"], ref["mu"])
+
+
+@pytest.mark.parametrize("variant", ["quad3", "lane4"])
+def test_server_job_equals_engine_cem(built, variant):
+    """A server job and the single-job engine CEM give bitwise-identical results: both launch
+    the one compiled rollout kernel of items.cu (the engine on a table of one slot) and share
+    the finalize, sample and refit code."""
+    ids = [0, 1, 2, 4]
+    job, (init, actions, target) = _job(4, 32, 6, 128, ids, 21, iters=5)
+    r = _run(_server(variant, max_slots=4, max_samples=128), [(job, None)])[21]
+    _assert_same(r, _engine_cem(variant, init, actions, target, 128, ids, 104, 21, 5))
+
+
+@pytest.mark.parametrize("variant", ["quad3", "lane4"])
+def test_served_equals_plain_with_more_jobs_than_slots(built, variant):
+    """Eleven jobs of uneven population, ragged window counts, horizons and parameter sets
+    through a three-slot server under a small work cap (jobs wait, slots are reused, several
+    rounds per tick) equal the same jobs run one at a time on the engine, bit for bit."""
+    rng = np.random.default_rng(8)
+    specs = []
+    for k in range(11):
+        W = int(rng.integers(5, 70))
+        H = int(rng.integers(2, 9))
+        N = int(rng.choice([32, 96, 160, 256]))
+        P = int(rng.integers(1, 14))
+        ids = sorted(rng.choice(13, P, replace=False).tolist())
+        specs.append((20 + k, W, H, N, ids, 40 + k, int(rng.integers(1, 4))))
+    jobs = {s[5]: _job(*s[:6], iters=s[6]) for s in specs}
+    srv = _server(variant, max_slots=3, max_samples=256)
+    srv.set_rounds(3)
+    srv.set_work_cap(64)
+    pending = list(jobs)
+    out = {}
+    while len(out) < len(jobs):
+        while pending and srv.submit(jobs[pending[0]][0]) is not None:
+            pending.pop(0)
+        active, _ = srv.stats()
+        srv.tick()
+        if not active:
+            srv.wait()
+        for r in srv.poll():
+            out[r["job_id"]] = r
+    for seed, W, H, N, ids, job_id, iters in specs:
+        init, actions, target = jobs[job_id][1]
+        _assert_same(out[job_id], _engine_cem(variant, init, actions, target, N, ids, 100 + seed, job_id, iters))
 
 
 def test_layout_switch_refused_while_jobs_are_held(built):
