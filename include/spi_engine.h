@@ -259,12 +259,12 @@ int spi_fd_fisher(spi_engine* e, const float* x0, const float* actions, const fl
  * Many sysid jobs of uneven population, window count, horizon and parameter dimension share
  * the GPU. Each job is one CEM identification (the work of scripts/mass_opt.py per dataset);
  * jobs are admitted into slots against an HBM budget as they arrive, every tick advances
- * every active job by one CEM iteration in one persistent rollout launch (work items are
- * (job, theta, 8-window group), claimed longest-horizon first), and finished jobs free their
- * slot and memory for the next arrivals. One tick is captured once as a CUDA graph. A job's
- * results do not depend on the other jobs in the mix (each work item runs the same code on
- * the same inputs wherever it is scheduled). No counterpart in the reference, which runs
- * one job at a time. */
+ * every active job by one CEM iteration in one rollout launch (work items are (job, theta,
+ * 8-window group), one warp each, laid out longest horizon first), and finished jobs free
+ * their slot and memory for the next arrivals. One tick is captured once as a CUDA graph. A
+ * job's results do not depend on the other jobs in the mix, and equal the single-job engine's
+ * (spi_cem_*) bit for bit: the server and spi_run launch the same compiled rollout kernel.
+ * No counterpart in the reference, which runs one job at a time. */
 typedef struct spi_server spi_server;
 
 typedef struct spi_job {
@@ -315,7 +315,9 @@ int spi_server_stats(spi_server* s, int32_t* active, size_t* bytes_free);
  * running more jobs at once only slows each of them down; shortest-remaining-work order
  * lets a short job that arrives during a long one finish first. */
 int spi_server_set_work_cap(spi_server* s, long long max_items);
-/* Persistent-grid shape: CTAs per SM (0 = occupancy maximum) and work items claimed per atomic. */
+/* Rollout-launch shape: ctas_per_sm > 0 caps a launch at that many CTAs per SM (each warp then
+ * takes as many consecutive work items as the cap requires); 0 = one warp per claim, no cap.
+ * items_per_claim: consecutive work items per warp (1 .. 64). */
 int spi_server_config(spi_server* s, int ctas_per_sm, int items_per_claim);
 /* Rollout-kernel occupancy variant (the launch-bounds CTAs per SM: 3 or 4 in the quad layout,
  * 2 to 4 in the lane layout), as spi_set_kernel_config. */

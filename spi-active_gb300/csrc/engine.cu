@@ -1,7 +1,6 @@
 // engine.cu -- C ABI of the batched candidate-evaluation engine (declared in spi_engine.h).
 #include <cuda_runtime.h>
 
-#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -51,17 +50,6 @@ __global__ void fill_f32(float* p, float v, long long n) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
 }
-// Resident CTAs of the engine's persistent rollout kernel (layout, min_blocks) on this device.
-int update_item_ctas(spi_engine* e) {
-  if (e->layout != SPI_LAYOUT_LANE && e->layout != SPI_LAYOUT_QUAD) return SPI_OK;
-  int dev = 0, sms = 0, occ = 0;
-  cudaError_t ce = cudaGetDevice(&dev);
-  if (ce == cudaSuccess) ce = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  if (ce == cudaSuccess) ce = items_occupancy(e->layout, e->min_blocks, &occ);
-  if (ce != cudaSuccess) return cuda_error(ce, "rollout kernel occupancy");
-  e->item_ctas = sms * std::max(occ, 1);
-  return SPI_OK;
-}
 }  // namespace
 
 int spi::run_impl(spi_engine* e, float* trace) {
@@ -81,7 +69,7 @@ int spi::run_impl(spi_engine* e, float* trace) {
   const unsigned grid = blocks_for(warps, 4);
   unsigned long long* bad = (unsigned long long*)e->bad.p;
   if (!trace && (e->layout == SPI_LAYOUT_LANE || e->layout == SPI_LAYOUT_QUAD)) {
-    // the server's persistent kernel on a table of one slot (items.h)
+    // the server's rollout kernel on a table of one slot (items.h), one warp per work item
     SlotDesc d{};
     d.win = win;
     d.theta = e->theta.f();
@@ -93,11 +81,12 @@ int spi::run_impl(spi_engine* e, float* trace) {
     d.norm = e->norm;
     d.active = 1;
     const long long items = items_of(e->layout, e->N, G);
-    const int ctas = (int)std::min<long long>((items + 3) / 4, std::max(e->item_ctas, 1));
+    const long long ctas = items_grid(items, 1);
+    if (ctas > 0x7fffffffLL) return set_error(SPI_EINVAL, "spi_run: %lld work items", items);
     SingleTable* tab = static_cast<SingleTable*>(e->items.p);
     cudaError_t ce = items_fill_single(tab, d, items, 1, e->stream);
     if (ce == cudaSuccess)
-      ce = items_launch(e->layout, e->min_blocks, e->host_model, e->d_model, single_tables(tab), 0, ctas, bad,
+      ce = items_launch(e->layout, e->min_blocks, e->host_model, e->d_model, single_tables(tab), 0, (int)ctas, bad,
                         e->stream);
     if (ce != cudaSuccess) return cuda_error(ce, "rollout launch");
   } else if (!trace && e->layout == SPI_LAYOUT_BLOCK) {
@@ -223,7 +212,7 @@ int spi_set_kernel_config(spi_engine* e, int min_blocks) {
     return set_error(SPI_EINVAL, "spi_set_kernel_config: min_blocks %d outside [%d, 5]", min_blocks, lo);
   e->min_blocks = min_blocks;
   if (e->graph_exec) { cudaGraphExecDestroy(e->graph_exec); e->graph_exec = nullptr; }
-  return update_item_ctas(e);
+  return SPI_OK;
 }
 
 int spi_set_kernel_layout(spi_engine* e, int layout) {
@@ -239,7 +228,7 @@ int spi_set_kernel_layout(spi_engine* e, int layout) {
   }
   e->layout = layout;
   if (e->graph_exec) { cudaGraphExecDestroy(e->graph_exec); e->graph_exec = nullptr; }
-  return update_item_ctas(e);
+  return SPI_OK;
 }
 
 int spi_set_cost(spi_engine* e, int mode, const float* sq_weights) {

@@ -24,7 +24,6 @@ struct spi_engine {
   int min_blocks = 3;                      // rollout kernel occupancy variant
   int layout = 0;                          // SPI_LAYOUT_QUAD / SPI_LAYOUT_LANE
   spi::DeviceBuf items;                    // one-slot work table of the rollout kernel (items.h)
-  int item_ctas = 0;                       // resident CTAs of that kernel on the device
   // CEM
   spi::DeviceBuf cem;                      // one CemState
   bool cem_ready = false;

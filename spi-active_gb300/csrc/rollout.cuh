@@ -27,6 +27,18 @@ struct WinView {
   int W, H;
 };
 
+// One job's buffers as the rollout kernels (and the server's finalize kernel) see them.
+struct SlotDesc {
+  WinView win;
+  float* theta;     // [N][SPI_THETA_DIM]
+  float* partial;   // [N][G][SPI_N_COMP]
+  float* comp;      // [N][SPI_N_COMP]
+  float* cost;      // [N]
+  int N, G;         // theta samples; eight-window groups, ceil(W / 8)
+  float norm;
+  int active;
+};
+
 __device__ __forceinline__ float qsum(float x) {
   x += __shfl_xor_sync(0xffffffffu, x, 1);
   x += __shfl_xor_sync(0xffffffffu, x, 2);

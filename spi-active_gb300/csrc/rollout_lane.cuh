@@ -126,34 +126,36 @@ __device__ __forceinline__ void substep_lane(const DevModel& M, BaseState<float>
 }
 
 // One warp: four consecutive items of the flattened list of (theta n, eight-window group g)
-// pairs, n * G + g for g < G = ceil(W / 8), starting at item g0; eight lanes per item, one
-// window each. Items may belong to different theta samples, so a window set with few windows
-// still fills the warp. Writes each item's weighted error components to
-// partial[(n G + g)][SPI_N_COMP]. theta: [N][SPI_THETA_DIM]. lane_smem: the CTA's
-// kLaneParkBytes of dynamic shared memory; bp_warp / gains_warp: the CTA's per-warp, per-item
-// parameter slots. MS: the motor shape (motor_shape_of the model, or kMotorRuntime).
-// Callable repeatedly by one warp (persistent kernels).
+// pairs of the job S, n * G + g for g < G = ceil(W / 8), starting at item g0; eight lanes per
+// item, one window each. Items may belong to different theta samples, so a window set with few
+// windows still fills the warp. Writes each item's weighted error components to
+// S->partial[(n G + g)][SPI_N_COMP]. lane_smem: the CTA's kLaneParkBytes of dynamic shared
+// memory; bp_warp / gains_warp: the CTA's per-warp, per-item parameter slots. MS: the motor
+// shape (motor_shape_of the model, or kMotorRuntime). Callable repeatedly by one warp.
+//
+// S lives in global memory (a slot table). Each field is read where it is needed, and the
+// fields used after the control-step loop are read again after a compiler memory barrier, so
+// that none of them holds a register through the loop: the loop then compiles as it does with
+// the fields in the kernel's parameter block (same FP32 instruction stream, no spills at the
+// 128-register cap).
 template <int MS = kMotorRuntime>
-__device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinView& win, const float* theta,
-                                                  long long g0, int N, float* partial, int G,
+__device__ __forceinline__ void rollout_lane_item(const DevModel& M, const SlotDesc* S, long long g0,
                                                   unsigned long long* n_bad, float4* lane_smem,
                                                   BaseParams<float> (*bp_warp)[4], float4 (*gains_warp)[4][8]) {
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, grp = lane >> 3, sub = lane & 7;
-  const int W = win.W, H = win.H;
-  const long long items = (long long)N * G;
-  long long q = g0 + grp;
-  const bool item_live = q < items;
-  if (!item_live) q = items - 1;
-  const int n = (int)(q / G), g = (int)(q % G);
-  int w = g * 8 + sub;
-  const bool active = item_live && w < W;
-  if (w >= W) w = W - 1;
-
+  int w;                             // this lane's window (clamped into the set)
   __syncwarp();                      // the warp's previous item has finished with its slots
   {
+    const int W = S->win.W, G = S->G;
+    const long long items = (long long)S->N * G;
+    long long q = g0 + grp;
+    if (q >= items) q = items - 1;
+    const int n = (int)(q / G), g = (int)(q % G);
+    w = min(g * 8 + sub, W - 1);
+    const float* theta = S->theta + (size_t)n * SPI_THETA_DIM;
     float th[SPI_THETA_DIM];
 #pragma unroll
-    for (int i = 0; i < SPI_THETA_DIM; ++i) th[i] = __ldg(theta + (size_t)n * SPI_THETA_DIM + i);
+    for (int i = 0; i < SPI_THETA_DIM; ++i) th[i] = __ldg(theta + i);
     if (sub == 0) bp_warp[wib][grp] = base_params<float>(M, th);
     if (sub < 4) store_gains(leg_gains(M, leg_params<float>(th, sub), sub), gains_warp[wib][grp] + 2 * sub);
     __syncwarp();
@@ -162,27 +164,42 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
   const LaneSlots sl = LaneSlots::of(lane_smem);
   BaseState<float> B;
   {
+    const float* init = S->win.init;
+    const int W = S->win.W;
     float s13[13];
 #pragma unroll
-    for (int i = 0; i < 13; ++i) s13[i] = __ldg(win.init + i * W + w);
+    for (int i = 0; i < 13; ++i) s13[i] = __ldg(init + i * W + w);
     base_from_world(B, s13);
 #pragma unroll
     for (int leg = 0; leg < 4; ++leg) {
       LegState<float> L;
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        L.q[k] = __ldg(win.init + (13 + 3 * leg + k) * W + w);
-        L.qd[k] = __ldg(win.init + (25 + 3 * leg + k) * W + w);
+        L.q[k] = __ldg(init + (13 + 3 * leg + k) * W + w);
+        L.qd[k] = __ldg(init + (25 + 3 * leg + k) * W + w);
       }
       sl.put_leg_state(leg, L);
     }
   }
-  const int dec = M.decimation;
-  for (int h = 0; h < H; ++h) {
-    const float4* ap = reinterpret_cast<const float4*>(win.act + ((size_t)h * W + w) * 12);
-    sl.put_targets(M, __ldg(ap), __ldg(ap + 1), __ldg(ap + 2));
-    for (int s = 0; s < dec; ++s) substep_lane<MS>(M, B, sl, &bp_warp[wib][grp], gains_warp[wib][grp]);
+  {
+    const int dec = M.decimation;
+    const float* act = S->win.act;
+    const int W = S->win.W, H = S->win.H;
+    for (int h = 0; h < H; ++h) {
+      const float4* ap = reinterpret_cast<const float4*>(act + ((size_t)h * W + w) * 12);
+      sl.put_targets(M, __ldg(ap), __ldg(ap + 1), __ldg(ap + 2));
+      for (int s = 0; s < dec; ++s) substep_lane<MS>(M, B, sl, &bp_warp[wib][grp], gains_warp[wib][grp]);
+    }
   }
+  asm volatile("" ::: "memory");     // read the descriptor again below, do not keep it live above
+  const int W = S->win.W, G = S->G;
+  const long long items = (long long)S->N * G;
+  long long q = g0 + grp;
+  const bool item_live = q < items;
+  if (!item_live) q = items - 1;
+  const int n = (int)(q / G), g = (int)(q % G);
+  const bool active = item_live && g * 8 + sub < W;
+  const float* tgt = S->win.tgt;
   LegState<float> L[4];
 #pragma unroll
   for (int leg = 0; leg < 4; ++leg) L[leg] = sl.leg_state(leg);
@@ -193,7 +210,7 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
   bool finite = true;
 #pragma unroll
   for (int i = 0; i < 13; ++i) {
-    const float d = s13[i] - __ldg(win.tgt + i * W + w);
+    const float d = s13[i] - __ldg(tgt + i * W + w);
     finite = finite && isfinite(s13[i]);
     if (i < 3) sp += d * d; else if (i < 7) sq += d * d; else if (i < 10) sv += d * d; else sw += d * d;
   }
@@ -201,16 +218,16 @@ __device__ __forceinline__ void rollout_lane_warp(const DevModel& M, const WinVi
   for (int leg = 0; leg < 4; ++leg)
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const float dq = L[leg].q[k] - __ldg(win.tgt + (13 + 3 * leg + k) * W + w);
-      const float dqd = L[leg].qd[k] - __ldg(win.tgt + (25 + 3 * leg + k) * W + w);
+      const float dq = L[leg].q[k] - __ldg(tgt + (13 + 3 * leg + k) * W + w);
+      const float dqd = L[leg].qd[k] - __ldg(tgt + (25 + 3 * leg + k) * W + w);
       finite = finite && isfinite(L[leg].q[k]) && isfinite(L[leg].qd[k]);
       sj += dq * dq;
       sjd += dqd * dqd;
     }
   if (active && !finite) atomicAdd(n_bad, 1ull);
-  const float wt = active ? __ldg(win.weight + w) : 0.f;
+  const float wt = active ? __ldg(S->win.weight + w) : 0.f;
   const float comp[SPI_N_COMP] = {sqrtf(sp), sqrtf(sq), sqrtf(sj), sp, sq, sv, sw, sj, sjd};
-  float* out = partial + ((size_t)n * G + g) * SPI_N_COMP;
+  float* out = S->partial + ((size_t)n * G + g) * SPI_N_COMP;
 #pragma unroll
   for (int k = 0; k < SPI_N_COMP; ++k) {
     const float v = group8_sum(active ? comp[k] * wt : 0.f);

@@ -2,12 +2,13 @@
 //
 // Slots hold admitted jobs (windows in SoA layout, population, cost partials, CEM state).
 // A tick advances every active slot by one CEM iteration:
-//   memset(work counter) -> cem_sample_kernel (grid row per slot) -> the persistent rollout
-//   kernel of items.cu (each warp claims (slot, theta, 8-window group) work items from an
-//   atomic counter, ordered longest horizon first; the single-job engine launches the same
-//   kernel on a one-slot table) -> server_finalize_kernel -> cem_refit_kernel.
+//   cem_sample_kernel (grid row per slot) -> the rollout kernel of items.cu (one warp per
+//   (slot, theta, 8-window group) work item, items ordered longest horizon first; the
+//   single-job engine launches the same kernel on a one-slot table) -> server_finalize_kernel
+//   -> cem_refit_kernel.
 // The tick is captured once as a CUDA graph: every per-tick quantity (slot table, work
-// order, item count) lives in device buffers that the host refreshes before each launch.
+// order, item count) lives in device buffers that the host refreshes before each launch, and
+// each round's rollout grid (one warp per work item) is set on the instantiated graph.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -113,7 +114,6 @@ struct spi_server {
   int* h_rounds = nullptr;         // pinned
   TickInfo* d_info = nullptr;      // [kMaxRounds]
   TickInfo* h_info = nullptr;      // pinned
-  unsigned long long* d_counter = nullptr;   // [kMaxRounds]
   unsigned long long* d_bad = nullptr;
   CemState* d_cem = nullptr;
   CemState* h_cem_in = nullptr;    // pinned, per slot
@@ -122,7 +122,11 @@ struct spi_server {
   cudaEvent_t staging_free = nullptr;
   cudaEvent_t tick_done[2] = {nullptr, nullptr};   // at most two ticks in flight
   cudaGraphExec_t graph = nullptr;
-  int grid = 0, ctas_per_sm = 0, items_per_claim = 1;
+  cudaGraph_t graph_src = nullptr;          // the captured graph (its nodes address `graph`'s)
+  cudaGraphNode_t roll_node[kMaxRounds] = {};
+  cudaKernelNodeParams roll_params[kMaxRounds] = {};
+  int grid_cap = 0;                         // CTAs of a rollout launch at most (0: no cap)
+  int ctas_per_sm = 0, items_per_claim = 1;
   long long max_items = 0;         // admission cap on work items per tick (0: none)
   int min_blocks = 3;              // rollout kernel occupancy variant
   int layout = SPI_LAYOUT_QUAD;    // SPI_LAYOUT_QUAD or SPI_LAYOUT_LANE
@@ -144,6 +148,14 @@ bool server_busy(const spi_server* s) {
   return false;
 }
 
+void drop_graph(spi_server* s) {
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  if (s->graph_src) cudaGraphDestroy(s->graph_src);
+  s->graph = nullptr;
+  s->graph_src = nullptr;
+  for (auto& nd : s->roll_node) nd = nullptr;
+}
+
 void free_server(spi_server* s) {
   if (!s) return;
   if (s->stream || s->capture) cudaStreamSynchronize(s->stream);
@@ -151,13 +163,13 @@ void free_server(spi_server* s) {
     if (sl.mem) cudaFree(sl.mem);
     if (sl.done) cudaEventDestroy(sl.done);
   }
-  if (s->graph) cudaGraphExecDestroy(s->graph);
+  drop_graph(s);
   if (s->staging_free) cudaEventDestroy(s->staging_free);
   for (auto& ev : s->tick_done) if (ev) cudaEventDestroy(ev);
   if (s->capture) cudaStreamDestroy(s->capture);
   cudaFree(s->d_model); cudaFree(s->d_slots); cudaFree(s->d_order); cudaFree(s->d_info);
   cudaFree(s->d_begin); cudaFree(s->d_rounds);
-  cudaFree(s->d_counter); cudaFree(s->d_bad); cudaFree(s->d_cem);
+  cudaFree(s->d_bad); cudaFree(s->d_cem);
   cudaFreeHost(s->h_slots); cudaFreeHost(s->h_order); cudaFreeHost(s->h_info);
   cudaFreeHost(s->h_begin); cudaFreeHost(s->h_rounds);
   cudaFreeHost(s->h_cem_in); cudaFreeHost(s->h_cem_out); cudaFreeHost(s->h_zero);
@@ -166,15 +178,15 @@ void free_server(spi_server* s) {
 
 int enqueue_tick(spi_server* s) {
   const int rows = (s->max_samples + 127) / 128;
-  cudaError_t ce = cudaMemsetAsync(s->d_counter, 0, sizeof(unsigned long long) * kMaxRounds, s->stream);
-  if (ce != cudaSuccess) return cuda_error(ce, "tick: reset counters");
+  cudaError_t ce = cudaSuccess;
   int npad = 1;
   while (npad < s->max_samples) npad <<= 1;
   const float* w = s->sq_w;
   for (int r = 0; r < s->rounds; ++r) {
     cem_sample_kernel<<<dim3(rows, s->max_slots), 128, 0, s->stream>>>(s->d_cem, s->d_rounds, r);
-    const ItemTables t{s->d_slots, s->d_order, s->d_begin, s->d_info, s->d_counter, s->max_slots};
-    ce = items_launch(s->layout, s->min_blocks, s->host_model, s->d_model, t, r, s->grid, s->d_bad, s->stream);
+    // grid 1 at capture; each tick sets the round's grid on the instantiated graph
+    const ItemTables t{s->d_slots, s->d_order, s->d_begin, s->d_info, s->max_slots};
+    ce = items_launch(s->layout, s->min_blocks, s->host_model, s->d_model, t, r, 1, s->d_bad, s->stream);
     if (ce != cudaSuccess) return cuda_error(ce, "tick: rollout launch");
     server_finalize_kernel<<<dim3(rows, s->max_slots), 128, 0, s->stream>>>(s->d_slots, s->d_rounds, r, s->cost_mode,
                                                                             w[0], w[1], w[2], w[3], w[4], w[5]);
@@ -196,9 +208,34 @@ int build_graph(spi_server* s) {
   s->stream = user;
   if (rc) { if (g) cudaGraphDestroy(g); return rc; }
   if (ce != cudaSuccess) return cuda_error(ce, "server: end capture");
-  ce = cudaGraphInstantiate(&s->graph, g, 0);
-  cudaGraphDestroy(g);
-  if (ce != cudaSuccess) { s->graph = nullptr; return cuda_error(ce, "server: instantiate"); }
+  // the rollout node of each round, by its kernel's round argument
+  size_t n = 0;
+  ce = cudaGraphGetNodes(g, nullptr, &n);
+  std::vector<cudaGraphNode_t> nodes(n);
+  if (ce == cudaSuccess && n) ce = cudaGraphGetNodes(g, nodes.data(), &n);
+  int found = 0;
+  for (size_t i = 0; ce == cudaSuccess && i < n; ++i) {
+    cudaGraphNodeType type;
+    ce = cudaGraphNodeGetType(nodes[i], &type);
+    if (ce != cudaSuccess || type != cudaGraphNodeTypeKernel) continue;
+    cudaKernelNodeParams p;
+    ce = cudaGraphKernelNodeGetParams(nodes[i], &p);
+    if (ce != cudaSuccess || !items_is_rollout_kernel(p.func)) continue;
+    const int r = *static_cast<const int*>(p.kernelParams[2]);
+    if (r < 0 || r >= s->rounds || s->roll_node[r]) { ce = cudaErrorInvalidValue; break; }
+    s->roll_node[r] = nodes[i];
+    s->roll_params[r] = p;
+    ++found;
+  }
+  if (ce == cudaSuccess && found != s->rounds) ce = cudaErrorInvalidValue;
+  if (ce == cudaSuccess) ce = cudaGraphInstantiate(&s->graph, g, 0);
+  if (ce != cudaSuccess) {
+    s->graph = nullptr;
+    cudaGraphDestroy(g);
+    for (auto& nd : s->roll_node) nd = nullptr;
+    return cuda_error(ce, "server: graph");
+  }
+  s->graph_src = g;
   return SPI_OK;
 }
 
@@ -208,9 +245,8 @@ int resize_grid(spi_server* s) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const cudaError_t ce = items_occupancy(s->layout, s->min_blocks, &occ);
   if (ce != cudaSuccess) return cuda_error(ce, "server: occupancy");
-  const int per = s->ctas_per_sm > 0 ? std::min(s->ctas_per_sm, std::max(occ, 1)) : std::max(occ, 1);
-  s->grid = sms * per;
-  if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+  s->grid_cap = s->ctas_per_sm > 0 ? sms * std::min(s->ctas_per_sm, std::max(occ, 1)) : 0;
+  drop_graph(s);
   return SPI_OK;
 }
 
@@ -251,7 +287,6 @@ int spi_server_create(const spi_robot* robot, int max_slots, int max_samples, si
   SRV_TRY(cudaMemset(s->d_rounds, 0, sizeof(int) * max_slots));
   SRV_TRY(cudaMalloc(&s->d_info, sizeof(TickInfo) * kMaxRounds));
   SRV_TRY(cudaMemset(s->d_info, 0, sizeof(TickInfo) * kMaxRounds));
-  SRV_TRY(cudaMalloc(&s->d_counter, sizeof(unsigned long long) * kMaxRounds));
   SRV_TRY(cudaMalloc(&s->d_bad, sizeof(unsigned long long)));
   SRV_TRY(cudaMemset(s->d_bad, 0, sizeof(unsigned long long)));
   SRV_TRY(cudaMalloc(&s->d_cem, sizeof(CemState) * max_slots));
@@ -295,7 +330,7 @@ int spi_server_set_cost(spi_server* s, int mode, const float* sq_weights) {
   if (mode != 0 && mode != 1) return set_error(SPI_EINVAL, "spi_server_set_cost: mode %d", mode);
   s->cost_mode = mode;
   if (sq_weights) memcpy(s->sq_w, sq_weights, sizeof(s->sq_w));
-  if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+  drop_graph(s);
   return SPI_OK;
 }
 
@@ -328,7 +363,7 @@ int spi_server_set_rounds(spi_server* s, int rounds) {
   if (rounds < 1 || rounds > kMaxRounds)
     return set_error(SPI_EINVAL, "spi_server_set_rounds: rounds %d outside [1, %d]", rounds, kMaxRounds);
   s->rounds = rounds;
-  if (s->graph) { cudaGraphExecDestroy(s->graph); s->graph = nullptr; }
+  drop_graph(s);
   return SPI_OK;
 }
 
@@ -522,7 +557,12 @@ int spi_server_tick(spi_server* s) {
     }
     s->h_info[r].total = begin;
     s->h_info[r].n_order = n;
-    s->h_info[r].items_per_claim = s->items_per_claim;
+    // one claim per warp; under a CTA cap a warp's claim grows until the capped grid covers
+    // the round
+    long long per = s->items_per_claim;
+    if (s->grid_cap > 0) per = std::max(per, (begin + 4LL * s->grid_cap - 1) / (4LL * s->grid_cap));
+    if (per > 0x7fffffffLL) return set_error(SPI_EINVAL, "spi_server_tick: %lld work items", begin);
+    s->h_info[r].items_per_claim = (int)per;
   }
   const size_t tab = (size_t)s->rounds * s->max_slots;
   ce = cudaMemcpyAsync(s->d_slots, s->h_slots, sizeof(SlotDesc) * s->max_slots, cudaMemcpyHostToDevice, s->stream);
@@ -537,6 +577,15 @@ int spi_server_tick(spi_server* s) {
   if (ce != cudaSuccess) return cuda_error(ce, "spi_server_tick: upload table");
   int rc = build_graph(s);
   if (rc) return rc;
+  for (int r = 0; r < s->rounds; ++r) {   // one warp per claim of the round's work items
+    const long long g = std::max(items_grid(s->h_info[r].total, s->h_info[r].items_per_claim), 1LL);
+    if (g > 0x7fffffffLL) return set_error(SPI_EINVAL, "spi_server_tick: %lld work items", s->h_info[r].total);
+    cudaKernelNodeParams& p = s->roll_params[r];
+    if (p.gridDim.x == (unsigned)g) continue;
+    p.gridDim = dim3((unsigned)g);
+    ce = cudaGraphExecKernelNodeSetParams(s->graph, s->roll_node[r], &p);
+    if (ce != cudaSuccess) return cuda_error(ce, "spi_server_tick: rollout grid");
+  }
   ce = cudaGraphLaunch(s->graph, s->stream);
   if (ce == cudaSuccess) ce = cudaEventRecord(s->tick_done[s->ticks & 1], s->stream);
   if (ce != cudaSuccess) return cuda_error(ce, "spi_server_tick: launch");

@@ -150,6 +150,23 @@ def test_rounds_per_tick_do_not_change_results(built, variant):
         assert np.array_equal(a["mu"], b["mu"])
 
 
+@pytest.mark.parametrize("variant", ["quad3", "lane4"])
+def test_launch_shape_does_not_change_results(built, variant):
+    """A rollout launch capped at one CTA per SM (each warp then takes many work items) and
+    three items per claim reach bitwise the same results as one warp per item."""
+    specs = [(9, 64, 12, 256, [0, 4], 51), (12, 40, 7, 128, list(range(13)), 54)]
+    res = {}
+    for shape in ((0, 1), (1, 3)):
+        s = _server(variant, max_slots=8, max_samples=256)
+        s.config(*shape)
+        res[shape] = _run(s, [_job(*sp, iters=3) for sp in specs])
+    for sp in specs:
+        a, b = res[(0, 1)][sp[-1]], res[(1, 3)][sp[-1]]
+        assert a["iterations"] == b["iterations"] == 3
+        assert np.array_equal(a["best_theta"], b["best_theta"]) and a["best_cost"] == b["best_cost"]
+        assert np.array_equal(a["mu"], b["mu"])
+
+
 def test_small_job_takes_several_iterations_per_tick(built):
     """Beside a job with 64x its work per iteration, a small job takes 4 iterations per tick."""
     s = _server("lane4", max_slots=4, max_samples=512)
