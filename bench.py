@@ -50,6 +50,9 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", choices=("c1", "c2", "c3", "c4", "rollout-case"), default="c1")
     ap.add_argument("--variant", default="lane4", help="rollout-case: rollout-kernel variant")
+    ap.add_argument("--c1-variant", default="auto",
+                    help="c1: rollout-kernel variant, or auto to time every variant on the workload first (under a "
+                         "profiler the timings that pick it are distorted: fix the variant the plain run chose)")
     ap.add_argument("--n-theta", type=int, default=1024, help="rollout-case: theta samples")
     ap.add_argument("--n-windows", type=int, default=256, help="rollout-case: windows")
     ap.add_argument("--horizon", type=int, default=20, help="rollout-case: control steps per window")
@@ -637,9 +640,13 @@ def run_ours(args):
     flush = torch.empty(256 * 1024 * 1024 // 4, device=dev)
     stream = torch.cuda.current_stream(dev)
     # pick the rollout-kernel occupancy variant on this workload (outside the timed region)
-    from spi_gb300.autotune import tune_engine
+    from spi_gb300.autotune import set_variant, tune_engine
     cem.sample()
-    variant, variant_ms = tune_engine(eng, use_cache=False)
+    if args.c1_variant == "auto":
+        variant, variant_ms = tune_engine(eng, use_cache=False)
+    else:
+        set_variant(eng, args.c1_variant)
+        variant, variant_ms = args.c1_variant, None
     cem.sample()             # the tuning runs do not advance the CEM state
 
     for _ in range(args.warmup):

@@ -2,7 +2,8 @@
 
 Jobs are CEM identifications over their own windows. They are admitted into
 slots against an HBM budget and advanced one CEM iteration per tick, all active
-jobs in one persistent rollout launch. Finished jobs free their slot and memory.
+jobs in one rollout launch (the same compiled kernel as the single-job engine, so a
+job's results equal the engine's bit for bit). Finished jobs free their slot and memory.
 """
 from __future__ import annotations
 
