@@ -29,6 +29,12 @@ __device__ __forceinline__ void philox4x32_10(uint32_t c[4], uint32_t k0, uint32
 }
 
 __device__ __forceinline__ double u01(uint32_t w) { return ((double)w + 0.5) * 2.3283064365386963e-10; }
+// -ln(u) for u = (w + 0.5) 2^-32 in FP32. Near u = 1 the logarithm is taken of the exact
+// complement, 1 - u = (2^32 - 1 - w + 0.5) 2^-32, so draws close to 1 keep their small radius.
+__device__ __forceinline__ float neg_log_u01f(uint32_t w) {
+  if (w < 0x80000000u) return -logf(((float)w + 0.5f) * 2.3283064e-10f);
+  return -log1pf(-((float)(0xFFFFFFFFu - w) + 0.5f) * 2.3283064e-10f);
+}
 
 // Orderable key: cost ascending (NaN last), then index ascending.
 __device__ __forceinline__ unsigned long long cost_key(float c, unsigned idx) {
@@ -44,49 +50,78 @@ __device__ __forceinline__ unsigned long long cost_key(float c, unsigned idx) {
 static __global__ void cem_sample_kernel(const CemState* __restrict__ st_all, const int* __restrict__ rounds = nullptr,
                                          int round = 0) {
   const CemState* st = st_all + blockIdx.y;
-  const int n = blockIdx.x * blockDim.x + threadIdx.x;
-  if (!st->active || n >= st->n_samples) return;
+  // exits uniform per CTA, before the barrier
+  if (!st->active || (int)(blockIdx.x * blockDim.x) >= st->n_samples) return;
   if (rounds && round >= rounds[blockIdx.y]) return;
-  float* theta = st->theta + (size_t)n * SPI_THETA_DIM;
   const int P = st->dim, it = st->iter;
-  const uint32_t k0 = (uint32_t)(st->seed & 0xFFFFFFFFull), k1 = (uint32_t)(st->seed >> 32);
-  double z[CEM_MAX_DIM + 3];
-#pragma unroll
-  for (int b = 0; b < (CEM_MAX_DIM + 3) / 4; ++b) {
-    if (4 * b >= P) break;
-    uint32_t c[4] = {(uint32_t)n, (uint32_t)it, (uint32_t)b, (uint32_t)st->job};
-    philox4x32_10(c, k0, k1);
-    if (it == 0) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) z[4 * b + q] = u01(c[q]);
-    } else {
-#pragma unroll
-      for (int q = 0; q < 2; ++q) {
-        const double u1 = u01(c[2 * q]), u2 = u01(c[2 * q + 1]);
-        const double r = sqrt(-2.0 * log(u1));
-        double s, co;
-        sincospi(2.0 * u2, &s, &co);
-        z[4 * b + 2 * q] = r * co;
-        z[4 * b + 2 * q + 1] = r * s;
-      }
-    }
+  // the distribution, staged once per CTA (as FP32 for the Gaussian draws), so that the
+  // per-dimension loops below read shared memory instead of waiting on global loads
+  __shared__ float s_L[CEM_MAX_DIM * CEM_MAX_DIM];
+  __shared__ float s_mu[CEM_MAX_DIM], s_lo[CEM_MAX_DIM], s_hi[CEM_MAX_DIM];
+  __shared__ float s_nom[SPI_THETA_DIM];
+  __shared__ int s_ids[CEM_MAX_DIM];
+  for (int i = threadIdx.x; i < P * CEM_MAX_DIM; i += blockDim.x) s_L[i] = (float)st->L[i];
+  for (int i = threadIdx.x; i < P; i += blockDim.x) {
+    s_mu[i] = (float)st->mu[i];
+    s_lo[i] = (float)st->lo[i];
+    s_hi[i] = (float)st->hi[i];
+    s_ids[i] = st->param_ids[i];
   }
+  for (int i = threadIdx.x; i < SPI_THETA_DIM; i += blockDim.x) s_nom[i] = st->nominal[i];
+  __syncthreads();
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= st->n_samples) return;
+  float* theta = st->theta + (size_t)n * SPI_THETA_DIM;
+  const uint32_t k0 = (uint32_t)(st->seed & 0xFFFFFFFFull), k1 = (uint32_t)(st->seed >> 32);
+  // Iteration 0 draws the uniform prior box in FP64 (no transcendental work). Later iterations
+  // draw Gaussians in FP32: Box-Muller and the Cholesky product are a few hundred operations
+  // per sample, which GB300's FP64 units would take tens of microseconds to finish, while the
+  // sample is stored as FP32 anyway (rounding to float commutes with the clamp to [lo, hi]).
   float out[SPI_THETA_DIM];
 #pragma unroll
-  for (int i = 0; i < SPI_THETA_DIM; ++i) out[i] = st->nominal[i];
-  for (int d = 0; d < P; ++d) {
-    double v;
-    if (it == 0) {
-      v = st->lo[d] + (st->hi[d] - st->lo[d]) * z[d];
-    } else {
-      v = st->mu[d];
-      for (int e = 0; e <= d; ++e) v += st->L[d * CEM_MAX_DIM + e] * z[e];
-      v = fmin(fmax(v, st->lo[d]), st->hi[d]);
-    }
-    const int slot = st->param_ids[d];
+  for (int i = 0; i < SPI_THETA_DIM; ++i) out[i] = s_nom[i];
+  if (it == 0) {
+    double z[CEM_MAX_DIM + 3];
 #pragma unroll
-    for (int i = 0; i < SPI_THETA_DIM; ++i)
-      if (i == slot) out[i] = (float)v;
+    for (int b = 0; b < (CEM_MAX_DIM + 3) / 4; ++b) {
+      if (4 * b >= P) break;
+      uint32_t c[4] = {(uint32_t)n, (uint32_t)it, (uint32_t)b, (uint32_t)st->job};
+      philox4x32_10(c, k0, k1);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) z[4 * b + q] = u01(c[q]);
+    }
+    for (int d = 0; d < P; ++d) {
+      const double v = st->lo[d] + (st->hi[d] - st->lo[d]) * z[d];
+      const int slot = s_ids[d];
+#pragma unroll
+      for (int i = 0; i < SPI_THETA_DIM; ++i)
+        if (i == slot) out[i] = (float)v;
+    }
+  } else {
+    float z[CEM_MAX_DIM + 3];
+#pragma unroll
+    for (int b = 0; b < (CEM_MAX_DIM + 3) / 4; ++b) {
+      if (4 * b >= P) break;
+      uint32_t c[4] = {(uint32_t)n, (uint32_t)it, (uint32_t)b, (uint32_t)st->job};
+      philox4x32_10(c, k0, k1);
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        const float r = sqrtf(2.0f * neg_log_u01f(c[2 * q]));
+        float sn, co;
+        sincospif(2.0f * (((float)c[2 * q + 1] + 0.5f) * 2.3283064e-10f), &sn, &co);
+        z[4 * b + 2 * q] = r * co;
+        z[4 * b + 2 * q + 1] = r * sn;
+      }
+    }
+    for (int d = 0; d < P; ++d) {
+      float v = s_mu[d];
+      for (int e = 0; e <= d; ++e) v = fmaf(s_L[d * CEM_MAX_DIM + e], z[e], v);
+      v = fminf(fmaxf(v, s_lo[d]), s_hi[d]);
+      const int slot = s_ids[d];
+#pragma unroll
+      for (int i = 0; i < SPI_THETA_DIM; ++i)
+        if (i == slot) out[i] = v;
+    }
   }
 #pragma unroll
   for (int i = 0; i < SPI_THETA_DIM; ++i) theta[i] = out[i];
