@@ -22,9 +22,7 @@ int cem_sample_impl(spi_engine* e) {
 }
 
 int cem_refit_impl(spi_engine* e) {
-  int npad = 1;
-  while (npad < e->N) npad <<= 1;
-  cem_refit_kernel<<<1, 1024, npad * sizeof(unsigned long long), e->stream>>>((CemState*)e->cem.p);
+  cem_refit_kernel<<<1, 1024, cem_refit_smem(e->N), e->stream>>>((CemState*)e->cem.p);
   cudaError_t ce = cudaGetLastError();
   return ce == cudaSuccess ? SPI_OK : cuda_error(ce, "cem_refit_kernel");
 }
@@ -94,7 +92,7 @@ int spi_cem_init(spi_engine* e, const spi_cem_config* c) {
   h.job = c->job_id;
   h.active = 1;
   cudaError_t ce = cudaFuncSetAttribute(cem_refit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        CEM_MAX_SAMPLES * (int)sizeof(unsigned long long));
+                                        kCemRefitMaxSmem);
   if (ce != cudaSuccess) return cuda_error(ce, "spi_cem_init: refit shared memory");
   int rc = e->cem.reserve(sizeof(CemState));
   if (rc) return rc;

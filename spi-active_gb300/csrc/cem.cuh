@@ -133,8 +133,21 @@ __device__ __forceinline__ double warp_sum_d(double v) {
   return v;
 }
 
+// Dynamic shared memory of cem_refit_kernel for a population of n: the selection keys
+// (8 bytes each) and the elite index list (4 bytes each).
+inline size_t cem_refit_smem(int n) { return (size_t)n * (sizeof(unsigned long long) + sizeof(int)); }
+constexpr int kCemRefitMaxSmem = CEM_MAX_SAMPLES * (int)(sizeof(unsigned long long) + sizeof(int));
+
 // One CTA (1024 threads) per state: elite select + mean / covariance + Cholesky. rounds as
-// in cem_sample_kernel.
+// in cem_sample_kernel. Dynamic shared memory: cem_refit_smem(n_samples) bytes.
+//
+// The elites are the n_elite smallest keys (cost ascending, NaN last, then index; keys are
+// unique). They are selected by radix select, 8 bits a pass from the top of the key: a pass
+// histograms the keys that share the bits decided so far, and the bin holding the target rank
+// fixes the next 8 bits. It stops when every key of that bin is an elite (at the latest when the
+// bin holds one key), typically after two to four passes over the cost bits, so the CTA meets
+// three barriers a pass instead of the ~36 of a full sort. The elites are then listed in index
+// order (a block-wide prefix sum), which fixes the order of the FP64 sums below.
 static __global__ void __launch_bounds__(1024) cem_refit_kernel(CemState* __restrict__ st_all,
                                                                const int* __restrict__ rounds = nullptr,
                                                                int round = 0) {
@@ -142,41 +155,103 @@ static __global__ void __launch_bounds__(1024) cem_refit_kernel(CemState* __rest
   extern __shared__ unsigned long long keys[];
   __shared__ double s_mu[CEM_MAX_DIM];
   __shared__ double s_cov[CEM_MAX_DIM * CEM_MAX_DIM];
+  __shared__ unsigned s_hist[256];
+  __shared__ unsigned long long s_prefix, s_mask, s_best;
+  __shared__ int s_rank, s_done;
+  __shared__ int s_scan[32];
   CemState* st = st_all + blockIdx.x;
   if (!st->active) return;   // uniform per CTA
   const float* theta = st->theta;
   const float* cost = st->cost;
   const int N = st->n_samples, P = st->dim, ne = st->n_elite;
-  int npad = 1;
-  while (npad < N) npad <<= 1;
-  for (int i = threadIdx.x; i < npad; i += blockDim.x)
-    keys[i] = i < N ? cost_key(cost[i], (unsigned)i) : ~0ull;
+  int* eidx = reinterpret_cast<int*>(keys + N);   // the elite index list, after the keys
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  // keys in index order, one contiguous run per thread
+  const int run = (N + blockDim.x - 1) / blockDim.x;
+  const int i0 = min(N, (int)threadIdx.x * run), i1 = min(N, i0 + run);
+  unsigned long long kmin = ~0ull;
+  for (int i = i0; i < i1; ++i) {
+    const unsigned long long k = cost_key(cost[i], (unsigned)i);
+    keys[i] = k;
+    kmin = k < kmin ? k : kmin;
+  }
+  // the best key (block minimum), for the best-so-far record
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long v = __shfl_xor_sync(0xffffffffu, kmin, o);
+    kmin = v < kmin ? v : kmin;
+  }
+  if (threadIdx.x == 0) { s_prefix = 0; s_mask = 0; s_rank = ne - 1; s_done = 0; s_best = ~0ull; }
   __syncthreads();
-  // bitonic sort, ascending. Thread t handles keys t, t + blockDim.x, ...; for a partner
-  // distance j < 32 both keys of a pair lie in one 32-key block that one warp handles, so a stage
-  // followed by such a stage orders with a warp barrier. A stage followed by one of distance
-  // >= 32 (every j >= 32, and the last stage j = 1 of a round k >= 32, whose successor has
-  // j = 2k / 2 >= 32) takes the CTA barrier.
-  for (int k = 2; k <= npad; k <<= 1) {
-    for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int i = threadIdx.x; i < npad; i += blockDim.x) {
-        const int l = i ^ j;
-        if (l > i) {
-          const unsigned long long a = keys[i], b = keys[l];
-          const bool up = (i & k) == 0;
-          if ((a > b) == up) { keys[i] = b; keys[l] = a; }
-        }
-      }
-      if (j >= 32 || (j == 1 && k >= 32)) __syncthreads(); else __syncwarp();
+  if (lane == 0) atomicMin(&s_best, kmin);
+  // radix select of the key of rank ne - 1
+  for (int shift = 56; shift >= 0; shift -= 8) {
+    for (int b = threadIdx.x; b < 256; b += blockDim.x) s_hist[b] = 0;
+    __syncthreads();
+    const unsigned long long prefix = s_prefix, mask = s_mask;
+    for (int i = i0; i < i1; ++i) {
+      const unsigned long long k = keys[i];
+      if ((k & mask) == prefix) atomicAdd(&s_hist[(unsigned)(k >> shift) & 0xFFu], 1u);
     }
+    __syncthreads();
+    if (warp == 0) {
+      const unsigned rank = (unsigned)s_rank;
+      unsigned c[8], sum = 0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) { c[q] = s_hist[8 * lane + q]; sum += c[q]; }
+      unsigned incl = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      const unsigned excl = incl - sum;
+      __syncwarp();
+      if (rank >= excl && rank < incl) {            // exactly one lane: its bins hold the rank
+        unsigned before = excl;
+        int q = 0;
+        while (rank >= before + c[q]) before += c[q++];
+        const unsigned r = rank - before;
+        s_prefix = prefix | ((unsigned long long)(8 * lane + q) << shift);
+        s_mask = mask | (0xFFull << shift);
+        s_rank = (int)r;
+        if (c[q] == r + 1) s_done = 1;              // every key of the bin is an elite
+      }
+    }
+    __syncthreads();
+    if (s_done) break;                              // uniform: read after the barrier
+  }
+  // elites: keys whose decided bits are below the final prefix, or equal to it
+  const unsigned long long fprefix = s_prefix, fmask = s_mask;
+  int cnt = 0;
+  for (int i = i0; i < i1; ++i) cnt += (keys[i] & fmask) <= fprefix ? 1 : 0;
+  int incl = cnt;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) s_scan[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int v = lane < nwarps ? s_scan[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += u;
+    }
+    s_scan[lane] = v;                                // inclusive warp totals
   }
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+  int pos = incl - cnt + (warp > 0 ? s_scan[warp - 1] : 0);
+  for (int i = i0; i < i1; ++i)
+    if ((keys[i] & fmask) <= fprefix) eidx[pos++] = i;
+  __syncthreads();
   // elite mean, one warp per dimension
   for (int d = warp; d < P; d += nwarps) {
     const int slot = st->param_ids[d];
     double s = 0.0;
-    for (int e = lane; e < ne; e += 32) s += (double)theta[(size_t)(keys[e] & 0xFFFFFFFFull) * SPI_THETA_DIM + slot];
+    for (int e = lane; e < ne; e += 32) s += (double)theta[(size_t)eidx[e] * SPI_THETA_DIM + slot];
     s = warp_sum_d(s);
     if (lane == 0) s_mu[d] = s / ne;
   }
@@ -195,7 +270,7 @@ static __global__ void __launch_bounds__(1024) cem_refit_kernel(CemState* __rest
     for (int t = threadIdx.x; t < m * P; t += blockDim.x) {
       const int e = t / P, d = t % P;
       s_c[e * CEM_MAX_DIM + d] =
-          (double)theta[(size_t)(keys[e0 + e] & 0xFFFFFFFFull) * SPI_THETA_DIM + st->param_ids[d]] - s_mu[d];
+          (double)theta[(size_t)eidx[e0 + e] * SPI_THETA_DIM + st->param_ids[d]] - s_mu[d];
     }
     __syncthreads();
 #pragma unroll
@@ -265,7 +340,7 @@ static __global__ void __launch_bounds__(1024) cem_refit_kernel(CemState* __rest
   }
   if (threadIdx.x == 0) {
     if (!s_ok) st->status = 1;
-    const unsigned b = (unsigned)(keys[0] & 0xFFFFFFFFull);
+    const unsigned b = (unsigned)(s_best & 0xFFFFFFFFull);
     const float bc = cost[b];
     if (bc < st->best_cost || (isnan(st->best_cost) && !isnan(bc))) {
       st->best_cost = bc;

@@ -78,7 +78,7 @@ int spi_search_create(const spi_cem_config* c, void* stream, spi_search** out) {
   h.theta = s->pop.f();
   h.cost = s->cost.f();
   cudaError_t ce = cudaFuncSetAttribute(cem_refit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        CEM_MAX_SAMPLES * (int)sizeof(unsigned long long));
+                                        kCemRefitMaxSmem);
   if (ce == cudaSuccess) ce = cudaMemcpyAsync(s->state.p, &h, sizeof(h), cudaMemcpyHostToDevice, s->stream);
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(s->stream);   // h lives on this stack
   if (ce != cudaSuccess) { delete s; return cuda_error(ce, "spi_search_create: upload"); }
@@ -113,9 +113,7 @@ int spi_search_refit(spi_search* s, const float* cost) {
   if (!s->sampled) return set_error(SPI_ESTATE, "spi_search_refit before spi_search_sample");
   cudaError_t ce = cudaMemcpyAsync(s->cost.p, cost, (size_t)s->n * 4, cudaMemcpyDeviceToDevice, s->stream);
   if (ce != cudaSuccess) return cuda_error(ce, "spi_search_refit: cost copy");
-  int npad = 1;
-  while (npad < s->n) npad <<= 1;
-  cem_refit_kernel<<<1, 1024, npad * sizeof(unsigned long long), s->stream>>>((CemState*)s->state.p);
+  cem_refit_kernel<<<1, 1024, cem_refit_smem(s->n), s->stream>>>((CemState*)s->state.p);
   ce = cudaGetLastError();
   if (ce != cudaSuccess) return cuda_error(ce, "spi_search_refit");
   s->sampled = false;

@@ -179,8 +179,6 @@ void free_server(spi_server* s) {
 int enqueue_tick(spi_server* s) {
   const int rows = (s->max_samples + 127) / 128;
   cudaError_t ce = cudaSuccess;
-  int npad = 1;
-  while (npad < s->max_samples) npad <<= 1;
   const float* w = s->sq_w;
   for (int r = 0; r < s->rounds; ++r) {
     cem_sample_kernel<<<dim3(rows, s->max_slots), 128, 0, s->stream>>>(s->d_cem, s->d_rounds, r);
@@ -190,7 +188,7 @@ int enqueue_tick(spi_server* s) {
     if (ce != cudaSuccess) return cuda_error(ce, "tick: rollout launch");
     server_finalize_kernel<<<dim3(rows, s->max_slots), 128, 0, s->stream>>>(s->d_slots, s->d_rounds, r, s->cost_mode,
                                                                             w[0], w[1], w[2], w[3], w[4], w[5]);
-    cem_refit_kernel<<<s->max_slots, 1024, npad * sizeof(unsigned long long), s->stream>>>(s->d_cem, s->d_rounds, r);
+    cem_refit_kernel<<<s->max_slots, 1024, cem_refit_smem(s->max_samples), s->stream>>>(s->d_cem, s->d_rounds, r);
   }
   ce = cudaGetLastError();
   return ce == cudaSuccess ? SPI_OK : cuda_error(ce, "tick: launch");
@@ -303,8 +301,7 @@ int spi_server_create(const spi_robot* robot, int max_slots, int max_samples, si
   SRV_TRY(cudaEventCreateWithFlags(&s->staging_free, cudaEventDisableTiming));
   SRV_TRY(cudaEventCreateWithFlags(&s->tick_done[0], cudaEventDisableTiming));
   SRV_TRY(cudaEventCreateWithFlags(&s->tick_done[1], cudaEventDisableTiming));
-  SRV_TRY(cudaFuncSetAttribute(cem_refit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               CEM_MAX_SAMPLES * (int)sizeof(unsigned long long)));
+  SRV_TRY(cudaFuncSetAttribute(cem_refit_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kCemRefitMaxSmem));
   for (auto& sl : s->slots) SRV_TRY(cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming));
 #undef SRV_TRY
   memset(s->h_slots, 0, sizeof(SlotDesc) * max_slots);

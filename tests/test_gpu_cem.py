@@ -53,6 +53,34 @@ def test_sampling_and_refit_match_oracle(built, P, N):
     np.testing.assert_allclose(th1[:, ids], ref1.astype(np.float32), rtol=2e-6, atol=1e-7)
 
 
+@pytest.mark.parametrize("n", [64, 1000, 4096, 16384])
+def test_refit_elite_selection_with_ties_and_nonfinite_costs(built, n):
+    """The refit's elite set under costs with many ties, NaN, +inf and -inf: the n_elite smallest
+    by (cost, index) with NaN after +inf, as the oracle orders them, at populations up to the
+    16384 maximum (the largest shared-memory footprint of the refit kernel)."""
+    from spi_gb300.active import DeviceSearch
+    P = 5
+    lo, hi = np.zeros(P), np.ones(P)
+    s = DeviceSearch(n, lo, hi, elite_frac=0.1, alpha=0.8, min_std_frac=1e-3, seed=5)
+    pop = s.sample()
+    theta = pop.cpu().numpy()[:, :P].astype(np.float64)
+    rng = np.random.default_rng(n)
+    cost = rng.integers(0, 7, n).astype(np.float32)          # seven distinct values: ties everywhere
+    cost[rng.choice(n, n // 10, replace=False)] = np.nan
+    cost[rng.choice(n, n // 20, replace=False)] = np.inf
+    cost[rng.choice(n, 3, replace=False)] = -np.inf
+    s.refit(torch.from_numpy(cost).cuda())
+    r = s.read()
+    mu0, cov0 = ocem.prior_moments(lo, hi)
+    mu, cov = ocem.refit(theta, cost, ocem.n_elite(n), mu0, cov0, 0.8, 1e-3 * (hi - lo))
+    np.testing.assert_allclose(r["mu"], mu, rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(r["cov"], cov, rtol=1e-9, atol=1e-15)
+    best = ocem.elite_order(cost)[0]
+    assert r["best_cost"] == -np.inf
+    np.testing.assert_array_equal(r["best"][:P], pop.cpu().numpy()[best, :P])
+    s.close()
+
+
 def test_graph_replay_equals_eager_steps(built):
     e1, c1, _ = _setup(P=4, N=512, seed=5)
     for _ in range(6):
