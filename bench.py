@@ -210,7 +210,7 @@ def _dist():
     return r, r.rank, r.world, r.local
 
 
-def served_vs_plain(specs, realtime, cfg=None, variant="lane4"):
+def served_vs_plain(specs, realtime, cfg=None, variant="lane3"):
     """Run the same jobs served (continuous batching) and plain (one job at a time), both on the
     rollout-kernel variant `variant`."""
     from spi_gb300.workloads import WindowBank, run_plain, run_served
@@ -257,7 +257,7 @@ def serving_mixes(args, variant, ceiling):
       alone leaves most SMs idle, the regime where batching raises throughput."""
     from spi_gb300.server import Server
     from spi_gb300.workloads import c2_specs, poisson_arrivals, small_specs
-    sv = variant if variant in Server.VARIANTS else "lane4"
+    sv = variant if variant in Server.VARIANTS else "lane3"
     n, it = args.mix_jobs, args.mix_iters
     out = {}
     mixes = (

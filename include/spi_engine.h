@@ -122,7 +122,7 @@ int spi_set_cost(spi_engine* e, int mode, const float* sq_weights);
  * other. */
 int spi_set_kernel_config(spi_engine* e, int min_blocks);
 
-/* Rollout-kernel lane layout (default after spi_create: SPI_LAYOUT_LANE with min_blocks 4).
+/* Rollout-kernel lane layout (default after spi_create: SPI_LAYOUT_LANE with min_blocks 3).
  * SPI_LAYOUT_QUAD: four lanes per rollout, one leg each, the base
  * solved on all four. SPI_LAYOUT_LANE: one lane per rollout through all four legs, the model
  * in the kernel's parameter block, 68 KB of shared memory per 128-thread CTA (three CTAs per

@@ -137,8 +137,8 @@ int spi_create(const spi_robot* robot, spi_engine** out) {
   if (!rc) rc = e->items.reserve(sizeof(SingleTable));
   if (rc) { cudaFree(e->d_model); delete e; return rc; }
   cudaMemset(e->bad.p, 0, sizeof(unsigned long long));
-  // default kernel: the lane layout at the 128-register cap (the fastest on the C1 workload)
-  if ((rc = spi_set_kernel_layout(e, SPI_LAYOUT_LANE)) || (rc = spi_set_kernel_config(e, 4))) {
+  // default kernel: the lane layout at the 168-register cap (the fastest on the C1 workload)
+  if ((rc = spi_set_kernel_layout(e, SPI_LAYOUT_LANE)) || (rc = spi_set_kernel_config(e, 3))) {
     spi_destroy(e);
     return rc;
   }

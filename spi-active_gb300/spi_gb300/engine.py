@@ -32,12 +32,12 @@ def _f32(t, shape, name, device):
 class Engine:
     """Batched evaluation of theta samples against logged windows (the C ABI's spi_engine).
 
-    variant: the rollout-kernel variant (see spi_gb300.autotune.VARIANTS). The default, lane4
-    (one lane per rollout, a 128-register cap, 3 CTAs per SM), is the fastest on the C1
+    variant: the rollout-kernel variant (see spi_gb300.autotune.VARIANTS). The default, lane3
+    (one lane per rollout, a 168-register cap, 3 CTAs per SM), is the fastest on the C1
     workload; spi_gb300.autotune.tune_engine times every variant on the caller's own batch."""
 
     def __init__(self, cfg: SimConfig | None = None, device=None, stream: torch.cuda.Stream | None = None,
-                 variant: str | None = "lane4"):
+                 variant: str | None = "lane3"):
         if not torch.cuda.is_available():
             raise RuntimeError("spi_gb300.Engine needs a CUDA device (no CPU fallback exists)")
         self.cfg = cfg or SimConfig()

@@ -145,7 +145,7 @@ def default_work_cap(device=None):
 
 
 def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=64, hbm_budget=150 << 30,
-               ctas_per_sm=0, items_per_claim=1, realtime=True, work_cap=None, variant="lane4", rounds=4,
+               ctas_per_sm=0, items_per_claim=1, realtime=True, work_cap=None, variant="lane3", rounds=4,
                timeline=True):
     """Continuous batching: admit on arrival while HBM budget, a slot and GPU work capacity are free;
     every tick advances each admitted job by 1 .. `rounds` CEM iterations (more for smaller jobs). Fisher requests are scored on a worker
@@ -239,7 +239,7 @@ def run_served(specs, bank: WindowBank, cfg: SimConfig | None = None, max_slots=
     return out
 
 
-def run_plain(specs, bank: WindowBank, cfg: SimConfig | None = None, graph=True, variant="lane4"):
+def run_plain(specs, bank: WindowBank, cfg: SimConfig | None = None, graph=True, variant="lane3"):
     """One job at a time through the single-job engine, in arrival order (FIFO), with the
     rollout-kernel variant the server runs (lane layout, 3 CTAs per SM by default)."""
     from .autotune import set_variant
