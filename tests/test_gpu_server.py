@@ -43,13 +43,15 @@ def test_same_result_alone_and_in_the_mix(built, variant):
         assert np.array_equal(r["mu"], alone["mu"])
 
 
-def _engine_cem(variant, init, actions, target, n, ids, seed, job_id, iters):
+def _engine_cem(variant, init, actions, target, n, ids, seed, job_id, iters, cost=None):
     from spi_gb300.autotune import set_variant
     from spi_gb300.cem import CEM
     from spi_gb300.engine import Engine
     e = Engine()
     e.load_windows(init, actions, target)
     set_variant(e, variant)
+    if cost is not None:
+        e.set_cost(*cost)
     cem = CEM(e, n_samples=n, param_ids=ids, lo=gm.THETA_PRIOR_LO[ids], hi=gm.THETA_PRIOR_HI[ids],
               nominal=gm.THETA_NOMINAL, seed=seed, job_id=job_id)
     cem.run(iters, graph=True)
@@ -72,6 +74,19 @@ def test_server_job_equals_engine_cem(built, variant):
     job, (init, actions, target) = _job(4, 32, 6, 128, ids, 21, iters=5)
     r = _run(_server(variant, max_slots=4, max_samples=128), [(job, None)])[21]
     _assert_same(r, _engine_cem(variant, init, actions, target, 128, ids, 104, 21, 5))
+
+
+@pytest.mark.parametrize("mode,weights", [(0, (10.0, 5.0, 0.1, 0.1, 1.0, 0.01)), (1, (3.0, 2.0, 0.5, 0.2, 4.0, 0.1))])
+def test_server_cost_settings_equal_engine_cem(built, mode, weights):
+    """The reference's norm cost (mode 0) and non-default squared-error weights: a server job
+    equals the engine CEM under the same cost settings bit for bit."""
+    from spi_gb300.server import Server
+    ids = [0, 3, 5, 9]
+    job, (init, actions, target) = _job(6, 29, 5, 96, ids, 31, iters=4)
+    srv = Server(max_slots=2, max_samples=128, cost_mode=mode, sq_weights=weights)
+    srv.set_variant("lane3")
+    r = _run(srv, [(job, None)])[31]
+    _assert_same(r, _engine_cem("lane3", init, actions, target, 96, ids, 106, 31, 4, cost=(mode, weights)))
 
 
 @pytest.mark.parametrize("variant", ["quad3", "lane4"])
